@@ -1,0 +1,290 @@
+"""Throughput of the fused NS+AD lattice-Boltzmann step on GB300 (one JSON line on rank 0).
+
+Workload (default): the 3D steady heat sink, coupled D3Q15 NS + D3Q15 advection-diffusion,
+160x160x80 lattice (2,048,000 nodes), FP32 populations and compute, Brinkman + natural
+convection collide (AD::MacroBrinkmanCollideNaturalConvection) with the production driver's
+boundary program (walls, Dirichlet T, heat-flux Q, corner/edge smoothing) every step, design
+from a seeded Gaussian random field (correlation length 8 cells). A bench "step" is one fused
+time step over the whole lattice: pull-stream + boundary program + collide. The population
+buffers (2 x 245 MB) exceed the 129 MB L2, so no flush is needed between steps.
+
+  value        MLUPS of the device-resident fused step (sum over ranks; replicas)
+  e2e          MLUPS through the C ABI with host buffers: per e2e step, upload alpha/kappa
+               from pinned host memory, run one residual-check interval of 100 time steps
+               (pl_solve), download T and u
+  roofline     HBM: 248 algorithmic bytes per node per step (read + write 2 x 15 FP32
+               populations, read alpha and kappa) / measured step time, vs MEASURED_PEAKS
+  cpu_baseline the C restatement of the reference's scalar OpenMP path (oracle/), FP64, on
+               the host cores, on a bounded number of steps of the same workload
+
+--impl reference times that CPU path alone (the reference's own implementation of the path
+cannot be built on the GPU host).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    "heatsink3d-160x160x80-fp32": dict(nd=3, lx=160, ly=160, lz=80, storage="fp32"),
+    "heatsink3d-192x192x96-fp32": dict(nd=3, lx=192, ly=192, lz=96, storage="fp32"),
+    "heatsink2d-1600x800-fp32": dict(nd=2, lx=1600, ly=800, lz=1, storage="fp32"),
+    "heatsink2d-1600x800-fp64": dict(nd=2, lx=1600, ly=800, lz=1, storage="fp64"),
+    "heatsink2d-1600x800-fp16": dict(nd=2, lx=1600, ly=800, lz=1, storage="fp16"),
+    "heatsink2d-1600x800-bf16": dict(nd=2, lx=1600, ly=800, lz=1, storage="bf16"),
+    "heatsink3d-160x160x80-fp16": dict(nd=3, lx=160, ly=160, lz=80, storage="fp16"),
+    "heatsink3d-160x160x80-bf16": dict(nd=3, lx=160, ly=160, lz=80, storage="bf16"),
+}
+DEFAULT = "heatsink3d-160x160x80-fp32"
+METRIC = "fused NS+AD MLUPS"
+
+
+def bytes_per_node(q, storage):
+    s = {"fp64": 8, "fp32": 4, "fp16": 2, "bf16": 2}[storage]
+    c = 8 if storage == "fp64" else 4
+    return 2 * 2 * q * s + 2 * c
+
+
+def setup(wl, seed=0):
+    from panslbm2_gb300 import heatsink as HS
+    p = HS.Params(wl["nd"], wl["lx"], wl["ly"], wl["lz"])
+    ss = HS.grf_design(wl["nd"], wl["lx"], wl["ly"], wl["lz"], seed=seed, sigma=8.0)
+    alpha, kappa, dads, dkds = p.design_fields(ss)
+    ops = HS.program_ops("forward", p)
+    return p, alpha, kappa, ops
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clock and throttle reasons during the timed region."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, dev):
+        self.dev, self.rows, self.proc = dev, [], None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm = [float(r[0]) for r in self.rows if len(r) >= 7 and r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if len(r) >= 7 and r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows if len(r) >= 7 for i in range(4) if r[3 + i] == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(sm)}
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def traffic_per_node(workload):
+    """DRAM bytes per node of the fused step from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "step_traffic.json")
+    try:
+        with open(path) as fh:
+            return json.load(fh).get(workload)
+    except Exception:
+        return None
+
+
+def cpu_port(p, alpha, kappa, ops, q, budget_s=12.0, max_steps=30):
+    """Time the oracle restatement of the reference's scalar OpenMP path (FP64) on the host."""
+    from oracle.olib import Oracle
+    from panslbm2_gb300 import _capi as A
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from _replay import replay
+    o = Oracle("oracle")
+    cores = os.cpu_count() or 1
+    o.set_threads(cores)
+    L = o.lat(q, p.lx, p.ly, p.lz)
+    n = p.lx * p.ly * p.lz
+    f, g = np.zeros((q, n)), np.zeros((q, n))
+    one, zero = np.ones(n), np.zeros(n)
+    o.init(L, 0, f, o.fields(rho=one, ux=zero, uy=zero, uz=zero))
+    o.init(L, 1, g, o.fields(tem=zero, ux=zero, uy=zero, uz=zero))
+    mac = {k: np.zeros(n) for k in ("rho", "ux", "uy", "uz", "tem", "qx", "qy", "qz")}
+    ph = dict(nu=p.nu, diff=0.0, gx=p.gx, gy=p.gy, gz=p.gz, tem0=p.tem0)
+    F = o.fields(alpha=alpha, diffusivity=kappa, **mac)
+
+    def one_step():
+        o.collide(L, A.AD_NATURAL, f, g, F, **ph, save=True)
+        o.stream(L, f)
+        o.stream(L, g)
+        replay(o, L, f, g, ops, n, ux=mac["ux"], uy=mac["uy"], uz=mac["uz"], kappa=kappa)
+
+    one_step()   # warm-up
+    t0, steps = time.perf_counter(), 0
+    while steps < max_steps and (time.perf_counter() - t0) < budget_s:
+        one_step()
+        steps += 1
+    dt = time.perf_counter() - t0
+    return {"value": n * steps / dt / 1e6, "unit": "MLUPS", "cores": cores, "kind": "port",
+            "sample": "%d full time steps (collide + 2 streams + boundary program) of the %dx%dx%d lattice, FP64"
+                      % (steps, p.lx, p.ly, p.lz)}
+
+
+def run_reference(args, wl):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    p, alpha, kappa, ops = setup(wl)
+    q = 9 if wl["nd"] == 2 else 15
+    cb = cpu_port(p, alpha, kappa, ops, q, budget_s=60.0, max_steps=max(1, min(args.steps, 40)))
+    line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "MLUPS", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded GRF design)",
+            "config": {"workload": args.workload, "nodes": p.lx * p.ly * p.lz, "backend": "cpu"},
+            "cpu_baseline": cb, "e2e": {"value": cb["value"], "unit": "MLUPS", "h2d_bytes_per_step": 0,
+                                        "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=50)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default=DEFAULT, choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    args = ap.parse_args()
+    wl = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        return run_reference(args, wl)
+
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from panslbm2_gb300 import _capi as A
+    from panslbm2_gb300 import heatsink as HS
+    from panslbm2_gb300.lattice import LatticePair, phys
+
+    p, alpha, kappa, ops = setup(wl, seed=rank)
+    q = 9 if wl["nd"] == 2 else 15
+    n = p.lx * p.ly * p.lz
+    zero, one = np.zeros(n), np.ones(n)
+    lp = LatticePair(q, p.lx, p.ly, p.lz, wl["storage"])
+    stream = torch.cuda.current_stream()
+    lp.set_stream(stream.cuda_stream)
+    lp.set_field(A.ALPHA, alpha)
+    lp.set_field(A.KAPPA, kappa)
+    lp.init(0, one, ux=zero, uy=zero, uz=zero)
+    lp.init(1, zero, ux=zero, uy=zero, uz=zero)
+    prog = lp.program(HS.to_descs(ops))
+    ph = phys(nu=p.nu, diff=0.0, gx=p.gx, gy=p.gy, gz=p.gz, tem0=p.tem0)
+    lp.collide(A.AD_NATURAL, ph)
+    lp.steps(A.AD_NATURAL, ph, prog, max(3, args.warmup))
+    torch.cuda.synchronize()
+    clocks = Clocks(local)
+    clocks.start()
+    time.sleep(0.3)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    _, l0 = lp.stats()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    lp.steps(A.AD_NATURAL, ph, prog, args.steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    ms = e0.elapsed_time(e1)
+    _, l1 = lp.stats()
+    ck = clocks.stop()
+    lp.synchronize()
+    tmax = ms
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        tmax = float(t.item())
+    ms_step = tmax / args.steps
+    value = world * n * args.steps / (tmax / 1e3) / 1e6
+
+    # end to end through the C ABI with pinned host buffers
+    ha = torch.from_numpy(alpha).pin_memory()
+    hk = torch.from_numpy(kappa).pin_memory()
+    outs = [torch.empty(n, dtype=torch.float64).pin_memory() for _ in range(1 + wl["nd"])]
+    out_ids = [A.TEM, A.UX, A.UY] + ([A.UZ] if wl["nd"] == 3 else [])
+    interval = 100
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        lp.set_field_ptr(A.ALPHA, ha.data_ptr())
+        lp.set_field_ptr(A.KAPPA, hk.data_ptr())
+        lp.solve(A.AD_NATURAL, ph, prog, max_steps=interval, check_every=interval, tol=0.0)
+        for fid, buf in zip(out_ids, outs):
+            lp.get_field_ptr(fid, buf.data_ptr())
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / args.e2e_steps
+    e2e = {"value": n * interval / e2e_s / 1e6, "unit": "MLUPS", "h2d_bytes_per_step": 2 * n * 8,
+           "d2h_bytes_per_step": len(outs) * n * 8, "time_steps_per_call": interval}
+
+    bpn = bytes_per_node(q, wl["storage"])
+    pop_mb = 2 * q * n * {"fp64": 8, "fp32": 4, "fp16": 2, "bf16": 2}[wl["storage"]] / 1e6
+    peak, src = peaks()
+    achieved = n * bpn / (ms_step / 1e3) / 1e9
+    tpn = traffic_per_node(args.workload)
+    roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "peak_source": src, "bytes_per_node": bpn,
+            "traffic": (tpn * n if tpn else None), "kernel": "fused step (interior + boundary kernels)"}
+    line = {"metric": METRIC, "value": round(value, 1), "unit": "MLUPS", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms_step, 5), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32" if wl["storage"] != "fp64" else "f64",
+            "data": "synthetic (seeded GRF design, correlation length 8)",
+            "config": {"workload": args.workload, "nodes": n, "storage": wl["storage"], "parallelism": "replicas",
+                       "l2": "inputs larger than L2: two population buffers of %.0f MB each" % pop_mb},
+            "roofline": roof, "e2e": e2e, "clocks": ck, "gpu_launches": int(l1 - l0)}
+    if rank == 0 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_port(p, alpha, kappa, ops, q)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    lp.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

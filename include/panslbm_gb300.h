@@ -1,0 +1,214 @@
+/*
+ * panslbm_gb300.h -- C ABI of the GB300 lattice-Boltzmann topology-optimisation library.
+ *
+ * The reference (PANSLBM2) is a header-only C++ template library with no FFI; its
+ * "interface" is the set of template functions the production drivers call. Each entry point
+ * below replaces one group of those calls; the C++ template layer in dropin/ (same header
+ * paths, namespaces and signatures as the reference) forwards to these symbols, and any other
+ * host language binds them directly. All pointers named `host*` are host
+ * memory; device memory is owned by the library and never crosses this boundary.
+ *
+ * Every call returns PL_OK (0) or a negative error code; pl_last_error() describes the last
+ * failure of the calling thread. Calls are asynchronous on the lattice's CUDA stream except
+ * where a host buffer is written (get / download calls synchronise).
+ */
+#ifndef PANSLBM_GB300_H
+#define PANSLBM_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PL_OK 0
+#define PL_ERR_ARG (-1)          /* invalid argument (size, kind, pointer)               */
+#define PL_ERR_CUDA (-2)         /* CUDA runtime error                                   */
+#define PL_ERR_UNSUPPORTED (-3)  /* kind / storage combination not built                 */
+#define PL_ERR_STATE (-4)        /* call order violated (e.g. snapshot before a collide) */
+#define PL_ERR_ALLOC (-5)        /* device allocation failed                             */
+#define PL_ERR_NONFINITE (-6)    /* non-finite value detected by a reduction             */
+
+/* pl_solve status */
+#define PL_CONVERGED 1
+#define PL_MAX_STEPS 2
+#define PL_DIVERGED 3
+
+/* population storage (compute is FP64 for PL_FP64, FP32 otherwise; 16-bit storage holds
+ * populations shifted by w_c * shift of their set) */
+#define PL_FP64 0
+#define PL_FP32 1
+#define PL_FP16 2
+#define PL_BF16 3
+
+/* collide kinds: one per reference collide routine */
+#define PL_NS_COLLIDE 0           /* NS::MacroCollide                         navierstokes.h:430-483   */
+#define PL_NS_BRINKMAN 1          /* NS::MacroBrinkmanCollide                 navierstokes.h:485-546   */
+#define PL_AD_NATURAL 2           /* AD::MacroBrinkmanCollideNaturalConvection advection.h:928-1044    */
+#define PL_AD_FORCE 3             /* AD::MacroBrinkmanCollideForceConvection  advection.h:812-926      */
+#define PL_AD_HEATEX 4            /* AD::MacroBrinkmanCollideHeatExchange     advection.h:714-810      */
+#define PL_AD_NATURAL_NOBRINK 5   /* AD::MacroCollideNaturalConvection        advection.h:616-712      */
+#define PL_AD_FORCE_NOBRINK 6     /* AD::MacroCollideForceConvection          advection.h:528-614      */
+#define PL_ANS_BRINKMAN 10        /* ANS::MacroBrinkmanCollide                adjointnavierstokes.h:396-470 */
+#define PL_AAD_NATURAL 11         /* AAD::MacroBrinkmanCollideNaturalConvection adjointadvection.h:1111-1230 */
+#define PL_AAD_FORCE 12           /* AAD::MacroBrinkmanCollideForceConvection adjointadvection.h:995-1109 */
+#define PL_AAD_HEATEX 13          /* AAD::MacroBrinkmanCollideHeatExchange    adjointadvection.h:892-993 */
+#define PL_AAD_MASSFLOW 14        /* AAD::MacroBrinkmanCollideNaturalConvectionMassFlow adjointadvection.h:1232-1355 */
+
+/* boundary-program op kinds */
+#define PL_BC_WALL 0      /* (D2Q9|D3Q15)::BoundaryConditionAlong*   type: 1 BARRIER, 2 MIRROR  */
+#define PL_BC_IWALL 1     /* (D2Q9|D3Q15)::iBoundaryConditionAlong*                             */
+#define PL_BC_NS_U 2      /* NS::BoundaryConditionSetUAlong*        v0,v1,v2 = ux,uy,uz          */
+#define PL_BC_NS_RHO 3    /* NS::BoundaryConditionSetRhoAlong*      v0 = rho, v1/v2 tangential   */
+#define PL_BC_AD_T 4      /* AD::BoundaryConditionSetTAlong*        v0 = T                       */
+#define PL_BC_AD_Q 5      /* AD::BoundaryConditionSetQAlong*        v0 = qn, per-node kappa      */
+#define PL_BC_AD_QC 6     /* AD::BoundaryConditionSetQAlong*        v0 = qn, constant `kappa`    */
+#define PL_BC_ANS_U 7     /* ANS::iBoundaryConditionSetUAlong*      v0..v2 = u, `eps`            */
+#define PL_BC_ANS_RHO 8   /* ANS::iBoundaryConditionSetRhoAlong*                                 */
+#define PL_BC_AAD_T 9     /* AAD::iBoundaryConditionSetTAlong*                                   */
+#define PL_BC_AAD_Q 10    /* AAD::iBoundaryConditionSetQAlong*      `eps`                        */
+#define PL_BC_AAD_RHO 11  /* AAD::iBoundaryConditionSetRhoAlong*    type: 1 SetT, 2 SetQ; `eps`  */
+#define PL_SMOOTH_CORNER 20  /* SmoothCorner()                                                   */
+#define PL_SMOOTH_AT 21      /* SmoothCornerAt(i,j[,k],di,dj[,dk])                               */
+#define PL_SMOOTH_LINE 22    /* SmoothCornerAlong{YZ,ZX,XY}: axis = 0,1,2; (i,j) = line, (di,dj)  */
+
+/* node fields exchanged with the host (double arrays of nx*ny*nz, idx = i + nx*(j + ny*k)) */
+#define PL_ALPHA 0   /* Brinkman resistance                         */
+#define PL_KAPPA 1   /* per-node diffusivity                        */
+#define PL_BETA 2    /* heat-exchange coefficient                   */
+#define PL_DIRX 3    /* mass-flow objective weights                 */
+#define PL_DIRY 4
+#define PL_DIRZ 5
+#define PL_RHO 8     /* forward macros stored by the last saving collide */
+#define PL_UX 9
+#define PL_UY 10
+#define PL_UZ 11
+#define PL_TEM 12
+#define PL_QX 13
+#define PL_QY 14
+#define PL_QZ 15
+#define PL_IP 16     /* adjoint macros stored by the last saving adjoint collide */
+#define PL_IUX 17
+#define PL_IUY 18
+#define PL_IUZ 19
+#define PL_IMX 20
+#define PL_IMY 21
+#define PL_IMZ 22
+#define PL_ITEM 23
+#define PL_IQX 24
+#define PL_IQY 25
+#define PL_IQZ 26
+#define PL_FWD_RHO 32   /* forward solution read by adjoint collides and adjoint BCs */
+#define PL_FWD_UX 33
+#define PL_FWD_UY 34
+#define PL_FWD_UZ 35
+#define PL_FWD_TEM 36
+
+typedef struct pl_lattice_s *pl_lattice;
+
+typedef struct {
+    double nu;            /* viscosity (BGK rate 1/(3 nu + 1/2))                */
+    double diff;          /* constant diffusivity of the siblings that take one  */
+    double gx, gy, gz;    /* buoyancy vector                                    */
+    double tem0;          /* reference temperature                              */
+} pl_phys;
+
+/* One boundary routine call, recorded in call order into a boundary program. Per-node
+ * selectors/values are full-lattice host arrays (the reference's functor of global (i,j,k)
+ * evaluated at every node); NULL selects 1 (walls: BARRIER) and NULL values use c0..c2. */
+typedef struct {
+    int kind;                 /* PL_BC_* or PL_SMOOTH_*                                  */
+    int lat;                  /* walls / smoothing: 0 NS set (pf), 1 AD set (pg)          */
+    int axis, pos, dir;       /* edge/face: axis 0/1/2, global position, side -1/+1      */
+    const int *type;
+    const double *v0, *v1, *v2;
+    double c0, c1, c2;
+    double eps, kappa;
+    int i, j, k, di, dj, dk;  /* smoothing arguments                                     */
+} pl_bc_desc;
+
+/* lattice pair (NS set + AD set) ---------------------------------------------------------
+ * replaces D2Q9<T>(lx, ly) / D3Q15<T>(lx, ly, lz) construction (d2q9.h:28-58,
+ * d3q15.h:28-86) for one particle pair pf/pg sharing a geometry. */
+int pl_create(int q, int nx, int ny, int nz, int storage, pl_lattice *out);
+int pl_destroy(pl_lattice h);
+const char *pl_last_error(void);
+int pl_synchronize(pl_lattice h);
+/* launch on a caller-owned CUDA stream (a cudaStream_t passed as void*; NULL = legacy default
+ * stream) instead of the lattice's own non-blocking stream */
+int pl_set_stream(pl_lattice h, void *stream);
+/* shift of 16-bit population storage, per set (default: f 1.0, g 0.0) */
+int pl_set_shift(pl_lattice h, double shift_f, double shift_g);
+
+/* populations: host buffer of q*N doubles, direction-major (p[c*N + idx]); set 0 = pf, 1 = pg */
+int pl_set_populations(pl_lattice h, int set, const double *host);
+int pl_get_populations(pl_lattice h, int set, double *host);
+
+/* node fields */
+int pl_set_field(pl_lattice h, int field, const double *host);
+int pl_get_field(pl_lattice h, int field, double *host);
+/* copy the forward macros of the last saving collide into PL_FWD_* */
+int pl_freeze_forward(pl_lattice h);
+
+/* boundary programs: the edge/face routines and smoothing of one time step, in call order
+ * (replaces the per-step BoundaryCondition* / SetT / SetQ / iSet* / SmoothCorner* calls) */
+int pl_program_create(pl_lattice h, const pl_bc_desc *descs, int n, int *prog);
+int pl_program_destroy(pl_lattice h, int prog);
+
+/* initial conditions: which 0 NS::InitialCondition(rho,u), 1 AD::(T,u), 2 ANS::(u; ip,iu),
+ * 3 AAD::(u; iT,iq). a0..a3 = the scalar/vector inputs, ux..uz = the velocity argument. */
+int pl_init(pl_lattice h, int which, const double *a0, const double *a1, const double *a2, const double *a3,
+            const double *ux, const double *uy, const double *uz);
+
+/* one collide in place (the reference's Macro*Collide* call) */
+int pl_collide(pl_lattice h, int kind, const pl_phys *ph, int save);
+/* one fused step: Stream/iStream + program `prog` (-1: none) + collide of kind */
+int pl_step(pl_lattice h, int kind, const pl_phys *ph, int prog, int save);
+/* n fused steps without saving (device-resident inner loop) */
+int pl_steps(pl_lattice h, int kind, const pl_phys *ph, int prog, int n);
+/* Stream + program without a collide. mode 0: Stream, 1: iStream (adjoint inputs),
+ * 2: program only (forward inputs), 3: program only (adjoint inputs); both_sets 0: pf only */
+int pl_stream(pl_lattice h, int mode, int prog, int both_sets);
+
+/* The reference driver loop (production/heatsink.cpp:142-174 forward, 183-212 adjoint):
+ * collide, then up to max_steps-1 fused steps, checking every `check_every` steps the
+ * residual (residual.h) of velocity and flux (forward) or adjoint velocity and flux
+ * (adjoint) against `tol`. Returns PL_OK and sets *status / *steps / res[0..1]. */
+int pl_solve(pl_lattice h, int kind, const pl_phys *ph, int prog, int max_steps, int check_every, double tol,
+             int *status, int *steps, double *res);
+
+/* snapshot of the g populations the last collide stored (gi / igi of the reference):
+ * slot 0 forward, 1 adjoint; host may be NULL (kept on the device for pl_sensitivity).
+ * host layout: snap[q*idx + c] (the reference's scalar layout). */
+int pl_snapshot(pl_lattice h, int slot, double *host);
+
+/* Residual(...) of residual.h over the current (a) and previous (b) saved macros:
+ * family 0 = (ux,uy[,uz]), 1 = (qx,qy[,qz]), 2 = (iux,iuy[,iuz]), 3 = (iqx,iqy[,iqz]). */
+int pl_residual(pl_lattice h, int family, double *out);
+/* Residual of arbitrary host arrays (ncomp of a, ncomp of b, n each) */
+int pl_residual_host(pl_lattice h, int n, int ncomp, const double *const *a, const double *const *b, double *out);
+
+/* sensitivities (dfds host array of N, accumulated into like the reference):
+ * which 0 AAD::SensitivityTemperatureAtHeatSource (adjointadvection.h:1495-1543, qn/mask per node)
+ *       1 AAD::SensitivityBrinkmanDiffusivity     (adjointadvection.h:1459-1493)
+ *       2 AAD::SensitivityHeatExchange            (adjointadvection.h:1443-1457, dkds = dbds)
+ *       3 ANS::SensitivityBrinkman                (adjointnavierstokes.h:540-554)
+ * reads PL_FWD_* (forward), the adjoint macros, PL_KAPPA and the two snapshots. */
+int pl_sensitivity(pl_lattice h, int which, double *dfds, const double *dads, const double *dkds, const double *qn,
+                   const int *mask);
+
+/* filters (heavisidefilter.h:404-899, densityfilter.h:10-515). mask: NULL = hat weight
+ * everywhere; else hat weight between two design cells (mask != 0), identity otherwise. */
+int pl_heaviside_var(pl_lattice h, double R, double beta, const double *s, const int *mask, double *out);
+int pl_heaviside_sens(pl_lattice h, double R, double beta, const double *s, const double *dfdrho, const int *mask,
+                      double *out);
+int pl_density_filter(pl_lattice h, double R, const double *v, const int *mask, double *out);
+/* Normalize (normalize.h:8-23), in place on a host array of n */
+int pl_normalize(pl_lattice h, double *v, int n);
+
+/* last step kernel time (ms) measured with CUDA events on the lattice stream, and number
+ * of kernels launched since creation */
+int pl_stats(pl_lattice h, double *last_step_ms, long long *launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

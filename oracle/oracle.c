@@ -86,7 +86,10 @@ static int refl_of(const lat_t *t, int c, int a) {
  *      D3Q15::Stream (d3q15.h:256-617, serial branch 601-614), iStream (619-980) ---- */
 void ol_stream(const ol_lat *L, double *f, int inverse) {
     lat_t T = mk(L); const lat_t *t = &T;
-    double *tmp = (double *)malloc(sizeof(double) * (size_t)t->n * (size_t)t->q);
+    static double *tmp = NULL;
+    static size_t cap = 0;
+    const size_t need = (size_t)t->n * (size_t)t->q;
+    if (need > cap) { free(tmp); tmp = (double *)malloc(sizeof(double) * need); cap = need; }
     int s = inverse ? 1 : -1;
 #pragma omp parallel for collapse(2)
     for (int k = 0; k < t->nz; ++k)
@@ -99,8 +102,7 @@ void ol_stream(const ol_lat *L, double *f, int inverse) {
                     F(tmp, c, idx) = F(f, c, src);
                 }
             }
-    memcpy(f, tmp, sizeof(double) * (size_t)t->n * (size_t)t->q);
-    free(tmp);
+    memcpy(f, tmp, sizeof(double) * need);
 }
 
 /* ---- face iteration helper: node (i,j,k) on the face axis=a at local position p ---- */

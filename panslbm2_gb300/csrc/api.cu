@@ -1,0 +1,986 @@
+// api.cu -- C ABI of the library (include/panslbm_gb300.h): lattice-pair handles, boundary
+// program compilation, fused step / solve loop, snapshots, sensitivities, filters.
+#include <cuda_runtime.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <cmath>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/panslbm_gb300.h"
+#include "common.h"
+#include "fields.h"
+#include "launch.h"
+
+using pl::KArgs;
+using pl::Op;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+#define CK(x)                                                                                     \
+    do {                                                                                          \
+        cudaError_t e_ = (x);                                                                     \
+        if (e_ != cudaSuccess) return fail(PL_ERR_CUDA, "%s: %s", #x, cudaGetErrorString(e_));    \
+    } while (0)
+
+struct Program {
+    bool valid = false;
+    int nb = 0, nops = 0, nslot = 0;
+    int *bnode = nullptr, *bstart = nullptr, *slot_of = nullptr;
+    Op *ops = nullptr;
+    uint8_t *flags = nullptr;
+    uint32_t face_mask = 0;
+};
+
+struct Taps {
+    int ntap = 0;
+    int *di = nullptr, *dj = nullptr, *dk = nullptr;
+    double *hat = nullptr;
+};
+
+typedef int (*LaunchFn)(int, int, bool, const KArgs &, cudaStream_t);
+typedef void (*AuxFn)(int, const KArgs &, int, const double *const *, int, int, double *, int, double, cudaStream_t);
+
+}  // namespace
+
+struct pl_lattice_s {
+    int q = 0, nd = 0, nx = 0, ny = 0, nz = 1, n = 0;
+    long long np = 0;
+    int storage = PL_FP32;
+    bool fp32 = true;
+    size_t ssize = 4, csize = 4;
+    cudaStream_t st = nullptr;
+    bool own_stream = false;
+    void *pop[2] = {nullptr, nullptr};
+    int cur = 0;
+    double shift_f = 1.0, shift_g = 0.0;
+    double *fld[48] = {nullptr};     // double fields by PL_* id (design inputs, forward solution)
+    void *cfld[11] = {nullptr};      // compute-type copies: alpha,kappa,beta,dirx,diry,dirz,frho,fux,fuy,fuz,ftem
+    double *fwd[2][8] = {{nullptr}};
+    double *adj[2][11] = {{nullptr}};
+    int fwd_next = 0, adj_next = 0;  // slot the next collide writes
+    int fwd_saved = -1, adj_saved = -1, fwd_prev_saved = -1, adj_prev_saved = -1;
+    int fwd_latest = -1;             // slot written by the last forward collide (boundary u)
+    std::vector<Program> progs;
+    double *snap[2] = {nullptr, nullptr};
+    // last collide, for snapshots
+    int last_kind = -1, last_src = -1, last_prog = -1, last_pull = 0, last_bcu_slot = -1;
+    pl_phys last_ph{};
+    // scratch
+    double *partial = nullptr;
+    int *nonfinite = nullptr;
+    double *dout = nullptr;
+    int *err = nullptr;
+    double *scratch[8] = {nullptr};
+    int *iscratch = nullptr;
+    std::map<std::pair<int, long long>, Taps> taps;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    double last_ms = 0.0;
+    long long launches = 0;
+    LaunchFn launch = nullptr;
+    AuxFn aux = nullptr;
+};
+
+namespace {
+
+LaunchFn pick_launch(int q, int s) {
+    if (q == 9) return s == PL_FP64 ? pl::launch_d2q9_f64 : s == PL_FP32 ? pl::launch_d2q9_f32 : s == PL_FP16 ? pl::launch_d2q9_f16 : pl::launch_d2q9_bf16;
+    return s == PL_FP64 ? pl::launch_d3q15_f64 : s == PL_FP32 ? pl::launch_d3q15_f32 : s == PL_FP16 ? pl::launch_d3q15_f16 : pl::launch_d3q15_bf16;
+}
+AuxFn pick_aux(int q, int s) {
+    if (q == 9) return s == PL_FP64 ? pl::aux_d2q9_f64 : s == PL_FP32 ? pl::aux_d2q9_f32 : s == PL_FP16 ? pl::aux_d2q9_f16 : pl::aux_d2q9_bf16;
+    return s == PL_FP64 ? pl::aux_d3q15_f64 : s == PL_FP32 ? pl::aux_d3q15_f32 : s == PL_FP16 ? pl::aux_d3q15_f16 : pl::aux_d3q15_bf16;
+}
+
+int dalloc(void **p, size_t bytes) {
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) { *p = nullptr; cudaGetLastError(); return fail(PL_ERR_ALLOC, "cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e)); }
+    return PL_OK;
+}
+int dzero(pl_lattice h, void *p, size_t bytes) {
+    CK(cudaMemsetAsync(p, 0, bytes, h->st));
+    return PL_OK;
+}
+int ensure_d(pl_lattice h, double **p, size_t count) {
+    if (*p) return PL_OK;
+    int r = dalloc((void **)p, sizeof(double) * count);
+    if (r) return r;
+    return dzero(h, *p, sizeof(double) * count);
+}
+int check_launch(pl_lattice h, int nk) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(PL_ERR_CUDA, "kernel launch: %s", cudaGetErrorString(e));
+    h->launches += nk;
+    return PL_OK;
+}
+bool valid_kind(int k) { return (k >= 0 && k <= 6) || (k >= 10 && k <= 14); }
+int field_index_c(int f) {
+    if (f >= PL_ALPHA && f <= PL_DIRZ) return f;
+    if (f >= PL_FWD_RHO && f <= PL_FWD_TEM) return 6 + (f - PL_FWD_RHO);
+    return -1;
+}
+// make sure a compute-type copy of field f exists and is current
+int sync_cfield(pl_lattice h, int f) {
+    int ci = field_index_c(f);
+    if (ci < 0) return PL_OK;
+    int r = ensure_d(h, &h->fld[f], h->n);
+    if (r) return r;
+    if (!h->cfld[ci]) { r = dalloc(&h->cfld[ci], h->csize * h->n); if (r) return r; }
+    pl::launch_to_compute(h->fld[f], h->cfld[ci], h->n, h->fp32, h->st);
+    return check_launch(h, 1);
+}
+int ensure_cfield(pl_lattice h, int f) {
+    int ci = field_index_c(f);
+    if (ci < 0) return fail(PL_ERR_ARG, "field %d has no compute copy", f);
+    if (h->cfld[ci]) return PL_OK;
+    return sync_cfield(h, f);
+}
+
+// ---- boundary program compilation ----------------------------------------------------------
+int node_id(pl_lattice h, int i, int j, int k) {
+    auto w = [](int v, int n) { return v == -1 ? n - 1 : (v == n ? 0 : v); };
+    return w(i, h->nx) + h->nx * (w(j, h->ny) + h->ny * (h->nd == 3 ? w(k, h->nz) : 0));
+}
+
+int compile_program(pl_lattice h, const pl_bc_desc *descs, int ndesc, Program &P) {
+    std::vector<Op> ops;
+    int seq = 0;
+    const int n[3] = {h->nx, h->ny, h->nz};
+    auto smooth_op = [&](int lat, int node, int a, int b, int c, int nn) {
+        Op o;
+        memset(&o, 0, sizeof o);
+        o.kind = pl::BC_SMOOTH; o.lat = (int8_t)lat; o.sub = (int8_t)nn; o.seq = seq; o.node = node;
+        o.nbr[0] = a; o.nbr[1] = b; o.nbr[2] = c;
+        ops.push_back(o);
+    };
+    auto smooth_at = [&](int lat, int i, int j, int k, int dx, int dy, int dz) {
+        if (i < 0 || i >= h->nx || j < 0 || j >= h->ny) return;
+        if (h->nd == 2) {
+            smooth_op(lat, node_id(h, i, j, 0), node_id(h, i - dx, j, 0), node_id(h, i, j - dy, 0), -1, 2);
+        } else {
+            if (k < 0 || k >= h->nz) return;
+            smooth_op(lat, node_id(h, i, j, k), node_id(h, i - dx, j, k), node_id(h, i, j - dy, k), node_id(h, i, j, k - dz), 3);
+        }
+    };
+    auto smooth_line = [&](int lat, int plane, int pa, int pb, int da, int db) {
+        if (h->nd != 3) return;
+        if (plane == 0) {
+            if (pa < 0 || pa >= h->ny || pb < 0 || pb >= h->nz) return;
+            for (int i = 0; i < h->nx; ++i)
+                smooth_op(lat, node_id(h, i, pa, pb), node_id(h, i, pa - da, pb), node_id(h, i, pa, pb - db), -1, 2);
+        } else if (plane == 1) {
+            if (pa < 0 || pa >= h->nz || pb < 0 || pb >= h->nx) return;
+            for (int j = 0; j < h->ny; ++j)
+                smooth_op(lat, node_id(h, pb, j, pa), node_id(h, pb, j, pa - da), node_id(h, pb - db, j, pa), -1, 2);
+        } else {
+            if (pa < 0 || pa >= h->nx || pb < 0 || pb >= h->ny) return;
+            for (int k = 0; k < h->nz; ++k)
+                smooth_op(lat, node_id(h, pa, pb, k), node_id(h, pa - da, pb, k), node_id(h, pa, pb - db, k), -1, 2);
+        }
+    };
+    for (int di = 0; di < ndesc; ++di) {
+        const pl_bc_desc &d = descs[di];
+        if (d.kind == PL_SMOOTH_CORNER) {
+            const int lx = h->nx, ly = h->ny, lz = h->nz, lat = d.lat;
+            if (h->nd == 2) {
+                smooth_at(lat, 0, 0, 0, -1, -1, 0); ++seq;
+                smooth_at(lat, 0, ly - 1, 0, -1, 1, 0); ++seq;
+                smooth_at(lat, lx - 1, 0, 0, 1, -1, 0); ++seq;
+                smooth_at(lat, lx - 1, ly - 1, 0, 1, 1, 0); ++seq;
+            } else {
+                // d3q15.h:199-220
+                smooth_line(lat, 0, 0, 0, -1, -1); ++seq;
+                smooth_line(lat, 0, ly - 1, 0, 1, -1); ++seq;
+                smooth_line(lat, 0, ly - 1, lz - 1, 1, 1); ++seq;
+                smooth_line(lat, 0, 0, lz - 1, -1, 1); ++seq;
+                smooth_line(lat, 1, 0, 0, -1, -1); ++seq;
+                smooth_line(lat, 1, lz - 1, 0, 1, -1); ++seq;
+                smooth_line(lat, 1, lz - 1, lx - 1, 1, 1); ++seq;
+                smooth_line(lat, 1, 0, lx - 1, -1, 1); ++seq;
+                smooth_line(lat, 2, 0, 0, -1, -1); ++seq;
+                smooth_line(lat, 2, lx - 1, 0, 1, -1); ++seq;
+                smooth_line(lat, 2, lx - 1, ly - 1, 1, 1); ++seq;
+                smooth_line(lat, 2, 0, ly - 1, -1, 1); ++seq;
+                smooth_at(lat, 0, 0, 0, -1, -1, -1); ++seq;
+                smooth_at(lat, lx - 1, 0, 0, 1, -1, -1); ++seq;
+                smooth_at(lat, lx - 1, ly - 1, 0, 1, 1, -1); ++seq;
+                smooth_at(lat, 0, ly - 1, 0, -1, 1, -1); ++seq;
+                smooth_at(lat, 0, 0, lz - 1, -1, -1, 1); ++seq;
+                smooth_at(lat, lx - 1, 0, lz - 1, 1, -1, 1); ++seq;
+                smooth_at(lat, lx - 1, ly - 1, lz - 1, 1, 1, 1); ++seq;
+                smooth_at(lat, 0, ly - 1, lz - 1, -1, 1, 1); ++seq;
+            }
+            continue;
+        }
+        if (d.kind == PL_SMOOTH_AT) { smooth_at(d.lat, d.i, d.j, d.k, d.di, d.dj, d.dk); ++seq; continue; }
+        if (d.kind == PL_SMOOTH_LINE) { smooth_line(d.lat, d.axis, d.i, d.j, d.di, d.dj); ++seq; continue; }
+        if (d.kind < PL_BC_WALL || d.kind > PL_BC_AAD_RHO)
+            return fail(PL_ERR_ARG, "program desc %d: unknown kind %d", di, d.kind);
+        if (d.axis < 0 || d.axis >= h->nd || (d.dir != -1 && d.dir != 1))
+            return fail(PL_ERR_ARG, "program desc %d: axis %d / dir %d invalid", di, d.axis, d.dir);
+        const int a = d.axis, p = d.pos;
+        if (p >= 0 && p < n[a]) {
+            const int b = (a + 1) % 3, c = (a + 2) % 3;
+            const int nb_ = (h->nd == 2 && b == 2) ? 1 : n[b], nc_ = (h->nd == 2 && c == 2) ? 1 : n[c];
+            int lat = 0;
+            if (d.kind == PL_BC_WALL || d.kind == PL_BC_IWALL) lat = d.lat;
+            else if (d.kind == PL_BC_AD_T || d.kind == PL_BC_AD_Q || d.kind == PL_BC_AD_QC || d.kind == PL_BC_AAD_T ||
+                     d.kind == PL_BC_AAD_Q) lat = 1;
+            for (int u = 0; u < nb_; ++u)
+                for (int v = 0; v < nc_; ++v) {
+                    int x[3]; x[a] = p; x[b] = u; x[c] = v;
+                    if (h->nd == 2) x[2] = 0;
+                    const int idx = x[0] + h->nx * (x[1] + h->ny * x[2]);
+                    const int t = d.type ? d.type[idx] : 1;
+                    if (d.kind == PL_BC_WALL || d.kind == PL_BC_IWALL) { if (t != 1 && t != 2) continue; }
+                    else if (t == 0) continue;
+                    Op o;
+                    memset(&o, 0, sizeof o);
+                    o.kind = d.kind; o.axis = (int8_t)a; o.dir = (int8_t)d.dir; o.lat = (int8_t)lat; o.sub = (int8_t)t;
+                    o.seq = seq; o.node = idx;
+                    // D3Q15 forward MIRROR on the +x side writes node (nx-1, j, k) (d3q15.h:1013)
+                    if (d.kind == PL_BC_WALL && h->nd == 3 && a == 0 && d.dir == 1 && t == 2)
+                        o.node = (h->nx - 1) + h->nx * (x[1] + h->ny * x[2]);
+                    o.v0 = d.v0 ? d.v0[idx] : d.c0;
+                    o.v1 = d.v1 ? d.v1[idx] : d.c1;
+                    o.v2 = d.v2 ? d.v2[idx] : d.c2;
+                    if (d.kind == PL_BC_AD_QC) o.v1 = d.kappa;
+                    o.eps = d.eps;
+                    o.nbr[0] = o.nbr[1] = o.nbr[2] = -1;
+                    ops.push_back(o);
+                }
+        }
+        ++seq;
+    }
+    // group by node, keep call order inside a node
+    std::stable_sort(ops.begin(), ops.end(), [](const Op &x, const Op &y) { return x.node < y.node; });
+    std::vector<int> slot_of(h->n, -1), bstart, opnodes;
+    for (size_t o = 0; o < ops.size(); ++o) {
+        if (o == 0 || ops[o].node != ops[o - 1].node) {
+            slot_of[ops[o].node] = (int)opnodes.size();
+            opnodes.push_back(ops[o].node);
+            bstart.push_back((int)o);
+        }
+    }
+    bstart.push_back((int)ops.size());
+    // skip mode: geometric when every op node lies on a domain face
+    auto on_face_bits = [&](int idx) {
+        const int i = idx % h->nx, r = idx / h->nx, j = r % h->ny, k = r / h->ny;
+        uint32_t m = 0;
+        if (i == 0) m |= 1; if (i == h->nx - 1) m |= 2; if (j == 0) m |= 4; if (j == h->ny - 1) m |= 8;
+        if (h->nd == 3) { if (k == 0) m |= 16; if (k == h->nz - 1) m |= 32; }
+        return m;
+    };
+    bool geometric = true;
+    uint32_t mask = 0;
+    for (int nd_ : opnodes) {
+        const uint32_t m = on_face_bits(nd_);
+        if (!m) { geometric = false; break; }
+        mask |= m;
+    }
+    std::vector<int> bnodes;
+    std::vector<uint8_t> flags;
+    if (geometric) {
+        for (int idx = 0; idx < h->n; ++idx) if (on_face_bits(idx) & mask) bnodes.push_back(idx);
+    } else {
+        bnodes = opnodes;
+        flags.assign(h->n, 0);
+        for (int nd_ : opnodes) flags[nd_] = 1;
+    }
+    P.nb = (int)bnodes.size();
+    P.nops = (int)ops.size();
+    P.nslot = (int)opnodes.size();
+    P.face_mask = geometric ? mask : 0;
+    int r;
+    if ((r = dalloc((void **)&P.slot_of, sizeof(int) * h->n))) return r;
+    CK(cudaMemcpyAsync(P.slot_of, slot_of.data(), sizeof(int) * h->n, cudaMemcpyHostToDevice, h->st));
+    if (P.nb) {
+        if ((r = dalloc((void **)&P.bnode, sizeof(int) * P.nb))) return r;
+        CK(cudaMemcpyAsync(P.bnode, bnodes.data(), sizeof(int) * P.nb, cudaMemcpyHostToDevice, h->st));
+    }
+    if ((r = dalloc((void **)&P.bstart, sizeof(int) * bstart.size()))) return r;
+    CK(cudaMemcpyAsync(P.bstart, bstart.data(), sizeof(int) * bstart.size(), cudaMemcpyHostToDevice, h->st));
+    if (P.nops) {
+        if ((r = dalloc((void **)&P.ops, sizeof(Op) * P.nops))) return r;
+        CK(cudaMemcpyAsync(P.ops, ops.data(), sizeof(Op) * P.nops, cudaMemcpyHostToDevice, h->st));
+    }
+    if (!geometric) {
+        if ((r = dalloc((void **)&P.flags, h->n))) return r;
+        CK(cudaMemcpyAsync(P.flags, flags.data(), h->n, cudaMemcpyHostToDevice, h->st));
+    }
+    CK(cudaStreamSynchronize(h->st));   // host vectors die here
+    P.valid = true;
+    return PL_OK;
+}
+
+void free_program(Program &P) {
+    cudaFree(P.bnode); cudaFree(P.bstart); cudaFree(P.slot_of); cudaFree(P.ops); cudaFree(P.flags);
+    P = Program();
+}
+
+// ---- kernel argument assembly ------------------------------------------------------------
+int build_args(pl_lattice h, int kind, const pl_phys *ph, int prog, int src, int dst, bool save, bool pull,
+               int bcu_slot, KArgs &a, bool kind_inputs = true) {
+    memset(&a, 0, sizeof a);
+    a.geo.nx = h->nx; a.geo.ny = h->ny; a.geo.nz = h->nz; a.geo.n = h->n; a.geo.np = h->np;
+    a.src = h->pop[src];
+    a.dst = dst >= 0 ? h->pop[dst] : nullptr;
+    a.ph.nu = ph ? ph->nu : 0.0; a.ph.diff = ph ? ph->diff : 0.0;
+    a.ph.gx = ph ? ph->gx : 0.0; a.ph.gy = ph ? ph->gy : 0.0; a.ph.gz = ph ? ph->gz : 0.0;
+    a.ph.tem0 = ph ? ph->tem0 : 0.0;
+    a.ph.shift_f = h->shift_f; a.ph.shift_g = h->shift_g;
+    a.pull = pull ? 1 : 0;
+    a.save = save ? 1 : 0;
+    a.err = h->err;
+    const bool adjk = pl::kind_is_adjoint(kind);
+    // inputs required by the kind
+    int r;
+    if (!kind_inputs) goto program;
+    if (kind == PL_NS_BRINKMAN || kind == PL_AD_NATURAL || kind == PL_AD_FORCE || kind == PL_AD_HEATEX || adjk) {
+        if (!h->fld[PL_ALPHA]) return fail(PL_ERR_STATE, "kind %d needs PL_ALPHA", kind);
+        if ((r = ensure_cfield(h, PL_ALPHA))) return r;
+        a.alpha = h->cfld[0];
+    }
+    if (pl::kind_node_kappa(kind)) {
+        if (!h->fld[PL_KAPPA]) return fail(PL_ERR_STATE, "kind %d needs PL_KAPPA", kind);
+        if ((r = ensure_cfield(h, PL_KAPPA))) return r;
+        a.kappa = h->cfld[1];
+    }
+    if (kind == PL_AD_HEATEX || kind == PL_AAD_HEATEX) {
+        if (!h->fld[PL_BETA]) return fail(PL_ERR_STATE, "kind %d needs PL_BETA", kind);
+        if ((r = ensure_cfield(h, PL_BETA))) return r;
+        a.beta = h->cfld[2];
+    }
+    if (kind == PL_AAD_MASSFLOW) {
+        for (int f = PL_DIRX; f <= (h->nd == 3 ? PL_DIRZ : PL_DIRY); ++f) {
+            if (!h->fld[f]) return fail(PL_ERR_STATE, "PL_AAD_MASSFLOW needs the direction fields");
+            if ((r = ensure_cfield(h, f))) return r;
+        }
+        a.dirx = h->cfld[3]; a.diry = h->cfld[4]; a.dirz = h->cfld[5];
+    }
+    if (adjk) {
+        for (int f = PL_FWD_RHO; f <= PL_FWD_TEM; ++f) {
+            if (f == PL_FWD_UZ && h->nd == 2) continue;
+            if (f == PL_FWD_TEM && kind == PL_ANS_BRINKMAN) continue;
+            if (!h->fld[f]) return fail(PL_ERR_STATE, "adjoint kind %d needs the forward solution (pl_freeze_forward)", kind);
+            if ((r = ensure_cfield(h, f))) return r;
+            a.fwd[f - PL_FWD_RHO] = h->cfld[6 + f - PL_FWD_RHO];
+        }
+    }
+    // macro outputs
+    if (!adjk) {
+        for (int m = 0; m < 8; ++m) { if ((r = ensure_d(h, &h->fwd[h->fwd_next][m], h->n))) return r; }
+        if (save) for (int m = 0; m < 8; ++m) a.out[m] = h->fwd[h->fwd_next][m];
+        a.bcu_out[0] = h->fwd[h->fwd_next][1]; a.bcu_out[1] = h->fwd[h->fwd_next][2]; a.bcu_out[2] = h->fwd[h->fwd_next][3];
+    } else {
+        for (int m = 0; m < 11; ++m) { if ((r = ensure_d(h, &h->adj[h->adj_next][m], h->n))) return r; }
+        if (save) for (int m = 0; m < 11; ++m) a.out[m] = h->adj[h->adj_next][m];
+    }
+program:
+    // boundary program
+    if (prog >= 0) {
+        if (prog >= (int)h->progs.size() || !h->progs[prog].valid) return fail(PL_ERR_ARG, "program %d invalid", prog);
+        const Program &P = h->progs[prog];
+        a.bnode = P.bnode; a.bstart = P.bstart; a.ops = P.ops; a.slot_of = P.slot_of; a.nb = P.nb;
+        a.geo.face_mask = P.face_mask; a.geo.flags = P.flags;
+        // velocity read by AD/AAD ops
+        if (!adjk) {
+            const int s = bcu_slot >= 0 ? bcu_slot : 0;
+            for (int m = 0; m < 3; ++m) { if ((r = ensure_d(h, &h->fwd[s][1 + m], h->n))) return r; }
+            a.bcu[0] = h->fwd[s][1]; a.bcu[1] = h->fwd[s][2]; a.bcu[2] = h->fwd[s][3];
+        } else {
+            for (int f = PL_FWD_RHO; f <= PL_FWD_TEM; ++f) { if ((r = ensure_d(h, &h->fld[f], h->n))) return r; }
+            a.bcu[0] = h->fld[PL_FWD_UX]; a.bcu[1] = h->fld[PL_FWD_UY]; a.bcu[2] = h->fld[PL_FWD_UZ];
+            a.bcrho = h->fld[PL_FWD_RHO]; a.bctem = h->fld[PL_FWD_TEM];
+        }
+        if ((r = ensure_d(h, &h->fld[PL_KAPPA], h->n))) return r;
+        a.bckappa = h->fld[PL_KAPPA];
+    } else {
+        a.slot_of = nullptr;
+        a.nb = 0;
+    }
+    if (!a.slot_of) {
+        // eval_node reads slot_of; give it an all -1 map
+        if (!h->iscratch) {
+            if ((r = dalloc((void **)&h->iscratch, sizeof(int) * h->n))) return r;
+            CK(cudaMemsetAsync(h->iscratch, 0xff, sizeof(int) * h->n, h->st));
+        }
+        a.slot_of = h->iscratch;
+    }
+    return PL_OK;
+}
+
+void after_collide(pl_lattice h, int kind, bool save, int src, int prog, bool pull, int bcu_slot, const pl_phys *ph) {
+    h->last_kind = kind; h->last_src = src; h->last_prog = prog; h->last_pull = pull ? 1 : 0;
+    h->last_bcu_slot = bcu_slot;
+    if (ph) h->last_ph = *ph;
+    if (!pl::kind_is_adjoint(kind)) {
+        h->fwd_latest = h->fwd_next;
+        if (save) { h->fwd_prev_saved = h->fwd_saved; h->fwd_saved = h->fwd_next; }
+        h->fwd_next ^= 1;
+    } else {
+        if (save) { h->adj_prev_saved = h->adj_saved; h->adj_saved = h->adj_next; }
+        h->adj_next ^= 1;
+    }
+}
+
+int do_collide(pl_lattice h, int kind, const pl_phys *ph, bool save) {
+    if (!valid_kind(kind)) return fail(PL_ERR_ARG, "unknown collide kind %d", kind);
+    const bool adjk = pl::kind_is_adjoint(kind);
+    if (!adjk) save = true;   // boundary ops of the next step read this velocity
+    KArgs a;
+    int r = build_args(h, kind, ph, -1, h->cur, h->cur ^ 1, save, false, -1, a);
+    if (r) return r;
+    if (h->launch(kind, pl::OP_COLLIDE, save, a, h->st)) return fail(PL_ERR_UNSUPPORTED, "kind %d not built for this storage", kind);
+    if ((r = check_launch(h, 1))) return r;
+    after_collide(h, kind, save, h->cur, -1, false, -1, ph);
+    h->cur ^= 1;
+    return PL_OK;
+}
+
+int do_step(pl_lattice h, int kind, const pl_phys *ph, int prog, bool save) {
+    if (!valid_kind(kind)) return fail(PL_ERR_ARG, "unknown collide kind %d", kind);
+    const int bcu_slot = h->fwd_latest;
+    KArgs a;
+    int r = build_args(h, kind, ph, prog, h->cur, h->cur ^ 1, save, true, bcu_slot, a);
+    if (r) return r;
+    if (h->launch(kind, pl::OP_STEP, save, a, h->st)) return fail(PL_ERR_UNSUPPORTED, "kind %d not built for this storage", kind);
+    if ((r = check_launch(h, a.nb > 0 ? 2 : 1))) return r;
+    after_collide(h, kind, save, h->cur, prog, true, bcu_slot, ph);
+    h->cur ^= 1;
+    return PL_OK;
+}
+
+int residual_family(pl_lattice h, int fam, double *out3, bool sync) {
+    const bool adjk = fam >= 2;
+    const int s = adjk ? h->adj_saved : h->fwd_saved, p = adjk ? h->adj_prev_saved : h->fwd_prev_saved;
+    if (s < 0 || p < 0 || s == p) return fail(PL_ERR_STATE, "residual needs two saved collides");
+    pl::ResidArgs ra;
+    memset(&ra, 0, sizeof ra);
+    ra.ncomp = h->nd;
+    ra.n = h->n;
+    for (int m = 0; m < h->nd; ++m) {
+        int fi;
+        if (fam == 0) fi = 1 + m; else if (fam == 1) fi = 5 + m; else if (fam == 2) fi = 1 + m; else fi = 8 + m;
+        ra.a[m] = adjk ? h->adj[s][fi] : h->fwd[s][fi];
+        ra.b[m] = adjk ? h->adj[p][fi] : h->fwd[p][fi];
+    }
+    const int nblk = pl::resid_blocks(h->n);
+    pl::launch_residual(ra, h->partial, nblk, h->nonfinite, h->dout + 3 * (fam & 1), h->st);
+    int r = check_launch(h, 2);
+    if (r) return r;
+    if (sync) {
+        CK(cudaMemcpyAsync(out3, h->dout + 3 * (fam & 1), sizeof(double) * 3, cudaMemcpyDeviceToHost, h->st));
+        CK(cudaStreamSynchronize(h->st));
+    }
+    return PL_OK;
+}
+
+int upload(pl_lattice h, double *dst, const double *host, size_t count) {
+    CK(cudaMemcpyAsync(dst, host, sizeof(double) * count, cudaMemcpyHostToDevice, h->st));
+    return PL_OK;
+}
+int download(pl_lattice h, double *host, const double *src, size_t count) {
+    CK(cudaMemcpyAsync(host, src, sizeof(double) * count, cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    return PL_OK;
+}
+
+Taps *get_taps(pl_lattice h, double R) {
+    long long key;
+    memcpy(&key, &R, sizeof key);
+    auto it = h->taps.find({h->nd, key});
+    if (it != h->taps.end()) return &it->second;
+    const int nR = (int)R;
+    std::vector<int> di, dj, dk;
+    std::vector<double> hat;
+    for (int a = -nR; a <= nR; ++a)
+        for (int b = -nR; b <= nR; ++b)
+            for (int c = -nR; c <= nR; ++c) {
+                const double dist = std::sqrt(std::pow((double)a, 2.0) + std::pow((double)b, 2.0) + std::pow((double)c, 2.0));
+                if (dist > R) continue;
+                if (h->nd == 2 && c != 0) continue;
+                di.push_back(a); dj.push_back(b); dk.push_back(c);
+                hat.push_back((R - dist) / R);
+            }
+    Taps t;
+    t.ntap = (int)di.size();
+    if (dalloc((void **)&t.di, sizeof(int) * t.ntap) || dalloc((void **)&t.dj, sizeof(int) * t.ntap) ||
+        dalloc((void **)&t.dk, sizeof(int) * t.ntap) || dalloc((void **)&t.hat, sizeof(double) * t.ntap))
+        return nullptr;
+    cudaMemcpy(t.di, di.data(), sizeof(int) * t.ntap, cudaMemcpyHostToDevice);
+    cudaMemcpy(t.dj, dj.data(), sizeof(int) * t.ntap, cudaMemcpyHostToDevice);
+    cudaMemcpy(t.dk, dk.data(), sizeof(int) * t.ntap, cudaMemcpyHostToDevice);
+    cudaMemcpy(t.hat, hat.data(), sizeof(double) * t.ntap, cudaMemcpyHostToDevice);
+    return &(h->taps[{h->nd, key}] = t);
+}
+
+int scratch(pl_lattice h, int i, double **p) {
+    int r = ensure_d(h, &h->scratch[i], h->n > 0 ? (size_t)h->n * (h->q) : 1);
+    *p = h->scratch[i];
+    return r;
+}
+
+}  // namespace
+
+// ==================================================================================== C ABI
+extern "C" {
+
+const char *pl_last_error(void) { return g_err.c_str(); }
+
+int pl_create(int q, int nx, int ny, int nz, int storage, pl_lattice *out) {
+    if (!out) return fail(PL_ERR_ARG, "out is NULL");
+    *out = nullptr;
+    if (q != 9 && q != 15) return fail(PL_ERR_ARG, "q must be 9 (D2Q9) or 15 (D3Q15), got %d", q);
+    if (nx < 2 || ny < 2 || (q == 15 && nz < 2)) return fail(PL_ERR_ARG, "lattice %dx%dx%d too small", nx, ny, nz);
+    if (storage < PL_FP64 || storage > PL_BF16) return fail(PL_ERR_ARG, "unknown storage %d", storage);
+    const long long n = (long long)nx * ny * (q == 15 ? nz : 1);
+    if (n > (1ll << 31) / 16) return fail(PL_ERR_ARG, "lattice of %lld nodes exceeds the 32-bit plane index", n);
+    // the boundary kernel replays smoothing chains with nested calls (about 1.3 KB of stack per
+    // thread); raise this context's per-thread stack limit when it is below that
+    size_t stack = 0;
+    if (cudaDeviceGetLimit(&stack, cudaLimitStackSize) == cudaSuccess && stack < 2048)
+        cudaDeviceSetLimit(cudaLimitStackSize, 2048);
+    cudaGetLastError();
+    pl_lattice h = new pl_lattice_s();
+    h->q = q; h->nd = q == 9 ? 2 : 3; h->nx = nx; h->ny = ny; h->nz = q == 9 ? 1 : nz; h->n = (int)n;
+    h->np = (n + 63) / 64 * 64;
+    h->storage = storage;
+    h->fp32 = storage != PL_FP64;
+    h->ssize = storage == PL_FP64 ? 8 : storage == PL_FP32 ? 4 : 2;
+    h->csize = h->fp32 ? 4 : 8;
+    h->launch = pick_launch(q, storage);
+    h->aux = pick_aux(q, storage);
+    int r = PL_OK;
+    if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess) {
+        delete h;
+        return fail(PL_ERR_CUDA, "cudaStreamCreate failed (no CUDA device?)");
+    }
+    h->own_stream = true;
+    const size_t popbytes = h->ssize * (size_t)h->np * 2 * q;
+    for (int b = 0; b < 2 && !r; ++b) r = dalloc(&h->pop[b], popbytes);
+    if (!r) r = dalloc((void **)&h->partial, sizeof(double) * 2 * 1024);
+    if (!r) r = dalloc((void **)&h->nonfinite, sizeof(int));
+    if (!r) r = dalloc((void **)&h->err, sizeof(int));
+    if (!r) r = dalloc((void **)&h->dout, sizeof(double) * 8);
+    if (r) { pl_destroy(h); return r; }
+    cudaMemsetAsync(h->pop[0], 0, popbytes, h->st);
+    cudaMemsetAsync(h->pop[1], 0, popbytes, h->st);
+    cudaMemsetAsync(h->nonfinite, 0, sizeof(int), h->st);
+    cudaMemsetAsync(h->err, 0, sizeof(int), h->st);
+    cudaEventCreate(&h->ev0);
+    cudaEventCreate(&h->ev1);
+    if (cudaStreamSynchronize(h->st) != cudaSuccess) { pl_destroy(h); return fail(PL_ERR_CUDA, "init failed"); }
+    *out = h;
+    return PL_OK;
+}
+
+int pl_destroy(pl_lattice h) {
+    if (!h) return PL_OK;
+    if (h->st) cudaStreamSynchronize(h->st);
+    for (auto &P : h->progs) free_program(P);
+    for (auto &kv : h->taps) { cudaFree(kv.second.di); cudaFree(kv.second.dj); cudaFree(kv.second.dk); cudaFree(kv.second.hat); }
+    cudaFree(h->pop[0]); cudaFree(h->pop[1]);
+    for (auto *p : h->fld) cudaFree(p);
+    for (auto *p : h->cfld) cudaFree(p);
+    for (int s = 0; s < 2; ++s) { for (auto *p : h->fwd[s]) cudaFree(p); for (auto *p : h->adj[s]) cudaFree(p); cudaFree(h->snap[s]); }
+    for (auto *p : h->scratch) cudaFree(p);
+    cudaFree(h->iscratch); cudaFree(h->partial); cudaFree(h->nonfinite); cudaFree(h->err); cudaFree(h->dout);
+    if (h->ev0) cudaEventDestroy(h->ev0);
+    if (h->ev1) cudaEventDestroy(h->ev1);
+    if (h->own_stream && h->st) cudaStreamDestroy(h->st);
+    delete h;
+    return PL_OK;
+}
+
+int pl_synchronize(pl_lattice h) {
+    if (!h) return fail(PL_ERR_ARG, "null handle");
+    CK(cudaStreamSynchronize(h->st));
+    int err = 0;
+    CK(cudaMemcpy(&err, h->err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (err) return fail(PL_ERR_STATE, "device reported error bits 0x%x (boundary program too deep)", err);
+    return PL_OK;
+}
+
+int pl_set_stream(pl_lattice h, void *stream) {
+    if (!h) return fail(PL_ERR_ARG, "null handle");
+    CK(cudaStreamSynchronize(h->st));
+    if (h->own_stream) cudaStreamDestroy(h->st);
+    h->st = static_cast<cudaStream_t>(stream);
+    h->own_stream = false;
+    return PL_OK;
+}
+
+int pl_set_shift(pl_lattice h, double sf, double sg) {
+    if (!h) return fail(PL_ERR_ARG, "null handle");
+    h->shift_f = sf;
+    h->shift_g = sg;
+    return PL_OK;
+}
+
+int pl_set_populations(pl_lattice h, int set, const double *host) {
+    if (!h || !host || (set != 0 && set != 1)) return fail(PL_ERR_ARG, "bad arguments");
+    double *buf;
+    int r = scratch(h, 0, &buf);
+    if (r) return r;
+    if ((r = upload(h, buf, host, (size_t)h->q * h->n))) return r;
+    KArgs a;
+    memset(&a, 0, sizeof a);
+    a.geo.n = h->n; a.geo.np = h->np; a.dst = h->pop[h->cur];
+    h->aux(pl::AUX_ENCODE, a, 0, nullptr, 0, 0, buf, set, set ? h->shift_g : h->shift_f, h->st);
+    return check_launch(h, 1);
+}
+
+int pl_get_populations(pl_lattice h, int set, double *host) {
+    if (!h || !host || (set != 0 && set != 1)) return fail(PL_ERR_ARG, "bad arguments");
+    double *buf;
+    int r = scratch(h, 0, &buf);
+    if (r) return r;
+    KArgs a;
+    memset(&a, 0, sizeof a);
+    a.geo.n = h->n; a.geo.np = h->np; a.src = h->pop[h->cur];
+    h->aux(pl::AUX_DECODE, a, 0, nullptr, 0, 0, buf, set, set ? h->shift_g : h->shift_f, h->st);
+    if ((r = check_launch(h, 1))) return r;
+    return download(h, host, buf, (size_t)h->q * h->n);
+}
+
+int pl_set_field(pl_lattice h, int f, const double *host) {
+    if (!h || !host) return fail(PL_ERR_ARG, "bad arguments");
+    int r;
+    if ((f >= PL_ALPHA && f <= PL_DIRZ) || (f >= PL_FWD_RHO && f <= PL_FWD_TEM)) {
+        if ((r = ensure_d(h, &h->fld[f], h->n))) return r;
+        if ((r = upload(h, h->fld[f], host, h->n))) return r;
+        return sync_cfield(h, f);
+    }
+    if (f >= PL_RHO && f <= PL_QZ) {
+        int s = h->fwd_saved >= 0 ? h->fwd_saved : 0;
+        if ((r = ensure_d(h, &h->fwd[s][f - PL_RHO], h->n))) return r;
+        if (h->fwd_saved < 0) { h->fwd_saved = s; h->fwd_latest = s; h->fwd_next = s ^ 1; }
+        return upload(h, h->fwd[s][f - PL_RHO], host, h->n);
+    }
+    if (f >= PL_IP && f <= PL_IQZ) {
+        int s = h->adj_saved >= 0 ? h->adj_saved : 0;
+        if ((r = ensure_d(h, &h->adj[s][f - PL_IP], h->n))) return r;
+        if (h->adj_saved < 0) { h->adj_saved = s; h->adj_next = s ^ 1; }
+        return upload(h, h->adj[s][f - PL_IP], host, h->n);
+    }
+    return fail(PL_ERR_ARG, "unknown field %d", f);
+}
+
+int pl_get_field(pl_lattice h, int f, double *host) {
+    if (!h || !host) return fail(PL_ERR_ARG, "bad arguments");
+    const double *src = nullptr;
+    if ((f >= PL_ALPHA && f <= PL_DIRZ) || (f >= PL_FWD_RHO && f <= PL_FWD_TEM)) src = h->fld[f];
+    else if (f >= PL_RHO && f <= PL_QZ) src = h->fwd_saved >= 0 ? h->fwd[h->fwd_saved][f - PL_RHO] : nullptr;
+    else if (f >= PL_IP && f <= PL_IQZ) src = h->adj_saved >= 0 ? h->adj[h->adj_saved][f - PL_IP] : nullptr;
+    else return fail(PL_ERR_ARG, "unknown field %d", f);
+    if (!src) return fail(PL_ERR_STATE, "field %d has no value yet", f);
+    return download(h, host, src, h->n);
+}
+
+int pl_freeze_forward(pl_lattice h) {
+    if (!h) return fail(PL_ERR_ARG, "null handle");
+    if (h->fwd_saved < 0) return fail(PL_ERR_STATE, "no saved forward collide");
+    static const int map[5] = {0, 1, 2, 3, 4};
+    int r;
+    for (int m = 0; m < 5; ++m) {
+        const int f = PL_FWD_RHO + m;
+        if ((r = ensure_d(h, &h->fld[f], h->n))) return r;
+        const double *src = h->fwd[h->fwd_saved][map[m]];
+        if (!src) continue;
+        CK(cudaMemcpyAsync(h->fld[f], src, sizeof(double) * h->n, cudaMemcpyDeviceToDevice, h->st));
+        if ((r = sync_cfield(h, f))) return r;
+    }
+    return PL_OK;
+}
+
+int pl_program_create(pl_lattice h, const pl_bc_desc *descs, int n, int *prog) {
+    if (!h || (!descs && n) || !prog) return fail(PL_ERR_ARG, "bad arguments");
+    Program P;
+    int r = compile_program(h, descs, n, P);
+    if (r) { free_program(P); return r; }
+    h->progs.push_back(P);
+    *prog = (int)h->progs.size() - 1;
+    return PL_OK;
+}
+
+int pl_program_destroy(pl_lattice h, int prog) {
+    if (!h || prog < 0 || prog >= (int)h->progs.size()) return fail(PL_ERR_ARG, "bad program");
+    cudaStreamSynchronize(h->st);
+    free_program(h->progs[prog]);
+    return PL_OK;
+}
+
+int pl_init(pl_lattice h, int which, const double *a0, const double *a1, const double *a2, const double *a3,
+            const double *ux, const double *uy, const double *uz) {
+    if (!h || which < 0 || which > 3 || !a0 || !ux || !uy || (h->nd == 3 && !uz)) return fail(PL_ERR_ARG, "bad arguments");
+    if (which >= 2 && (!a1 || !a2 || (h->nd == 3 && !a3))) return fail(PL_ERR_ARG, "adjoint init needs a1..a3");
+    double *buf;
+    int r = scratch(h, 1, &buf);   // q*N doubles >= 7*N
+    if (r) return r;
+    const double *hs[7] = {a0, a1, a2, a3, ux, uy, uz};
+    const double *in[7];
+    for (int m = 0; m < 7; ++m) {
+        double *d = buf + (size_t)m * h->n;
+        if (hs[m] && (m < 4 || m - 4 < h->nd)) { if ((r = upload(h, d, hs[m], h->n))) return r; }
+        else { CK(cudaMemsetAsync(d, 0, sizeof(double) * h->n, h->st)); }
+        in[m] = d;
+    }
+    KArgs a;
+    memset(&a, 0, sizeof a);
+    a.geo.n = h->n; a.geo.np = h->np; a.dst = h->pop[h->cur];
+    a.ph.shift_f = h->shift_f; a.ph.shift_g = h->shift_g;
+    h->aux(pl::AUX_INIT, a, which, in, 0, 0, nullptr, 0, 0.0, h->st);
+    if ((r = check_launch(h, 1))) return r;
+    return pl_synchronize(h);
+}
+
+int pl_collide(pl_lattice h, int kind, const pl_phys *ph, int save) {
+    if (!h || !ph) return fail(PL_ERR_ARG, "bad arguments");
+    return do_collide(h, kind, ph, save != 0);
+}
+
+int pl_step(pl_lattice h, int kind, const pl_phys *ph, int prog, int save) {
+    if (!h || !ph) return fail(PL_ERR_ARG, "bad arguments");
+    return do_step(h, kind, ph, prog, save != 0);
+}
+
+int pl_steps(pl_lattice h, int kind, const pl_phys *ph, int prog, int n) {
+    if (!h || !ph || n < 0) return fail(PL_ERR_ARG, "bad arguments");
+    CK(cudaEventRecord(h->ev0, h->st));
+    for (int t = 0; t < n; ++t) {
+        int r = do_step(h, kind, ph, prog, false);
+        if (r) return r;
+    }
+    CK(cudaEventRecord(h->ev1, h->st));
+    return PL_OK;
+}
+
+int pl_stream(pl_lattice h, int mode, int prog, int both_sets) {
+    if (!h || mode < 0 || mode > 3) return fail(PL_ERR_ARG, "bad arguments");
+    const bool inverse = mode == 1, nopull = mode >= 2, adjin = mode == 1 || mode == 3;
+    KArgs a;
+    int r = build_args(h, adjin ? PL_ANS_BRINKMAN : PL_NS_COLLIDE, nullptr, prog, h->cur, h->cur ^ 1, false, !nopull,
+                       h->fwd_latest, a, false);
+    if (r) return r;
+    h->aux(pl::AUX_STREAM_PROGRAM, a, 0, nullptr, both_sets, inverse ? 1 : -1, nullptr, 0, 0.0, h->st);
+    if ((r = check_launch(h, 1))) return r;
+    h->cur ^= 1;
+    h->last_kind = -1;
+    return PL_OK;
+}
+
+int pl_solve(pl_lattice h, int kind, const pl_phys *ph, int prog, int max_steps, int check_every, double tol,
+             int *status, int *steps, double *res) {
+    if (!h || !ph || max_steps < 1 || check_every < 1 || !status || !steps) return fail(PL_ERR_ARG, "bad arguments");
+    const bool adjk = pl::kind_is_adjoint(kind);
+    const int fa = adjk ? 2 : 0, fb = adjk ? 3 : 1;
+    const bool has_g = pl::kind_has_g(kind);
+    *status = PL_MAX_STEPS;
+    *steps = max_steps;
+    double r0[3] = {0, 0, 0}, r1[3] = {0, 0, 0};
+    CK(cudaMemsetAsync(h->nonfinite, 0, sizeof(int), h->st));
+    CK(cudaEventRecord(h->ev0, h->st));
+    int r;
+    for (int t = 1; t <= max_steps; ++t) {
+        const bool save = (t % check_every == 0) || (t % check_every == check_every - 1) || check_every == 1;
+        if (t == 1) r = do_collide(h, kind, ph, true);
+        else r = do_step(h, kind, ph, prog, save);
+        if (r) return r;
+        if (t % check_every == 0 && t > 1) {
+            if ((r = residual_family(h, fa, r0, false))) return r;
+            if (has_g && (r = residual_family(h, fb, r1, false))) return r;
+            double outv[6];
+            int bad = 0;
+            CK(cudaMemcpyAsync(outv, h->dout, sizeof(double) * 6, cudaMemcpyDeviceToHost, h->st));
+            CK(cudaMemcpyAsync(&bad, h->nonfinite, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+            CK(cudaStreamSynchronize(h->st));
+            r0[2] = outv[2];
+            r1[2] = has_g ? outv[5] : 0.0;
+            if (bad || !std::isfinite(r0[2]) || (has_g && !std::isfinite(r1[2]))) {
+                *status = PL_DIVERGED;
+                *steps = t;
+                break;
+            }
+            if (r0[2] < tol && (!has_g || r1[2] < tol)) {
+                *status = PL_CONVERGED;
+                *steps = t;
+                break;
+            }
+        }
+    }
+    CK(cudaEventRecord(h->ev1, h->st));
+    CK(cudaEventSynchronize(h->ev1));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+    h->last_ms = ms;
+    if (res) { res[0] = r0[2]; res[1] = r1[2]; }
+    return pl_synchronize(h);
+}
+
+int pl_snapshot(pl_lattice h, int slot, double *host) {
+    if (!h || (slot != 0 && slot != 1)) return fail(PL_ERR_ARG, "bad arguments");
+    if (h->last_kind < 0) return fail(PL_ERR_STATE, "no collide to take a snapshot of");
+    if (pl::kind_is_adjoint(h->last_kind) != (slot == 1)) return fail(PL_ERR_STATE, "last collide does not match slot %d", slot);
+    if (!pl::kind_has_snapshot(h->last_kind)) return fail(PL_ERR_STATE, "kind %d stores no snapshot", h->last_kind);
+    int r = ensure_d(h, &h->snap[slot], (size_t)h->q * h->np);
+    if (r) return r;
+    // the last collide read population buffer last_src; re-evaluate its input state
+    const int saved_next = pl::kind_is_adjoint(h->last_kind) ? h->adj_next : h->fwd_next;
+    KArgs a;
+    r = build_args(h, h->last_kind, &h->last_ph, h->last_prog, h->last_src, -1, false, h->last_pull != 0,
+                   h->last_bcu_slot, a);
+    (void)saved_next;
+    if (r) return r;
+    if (h->last_prog < 0) a.pull = 0;
+    a.snap = h->snap[slot];
+    if (h->launch(h->last_kind, pl::OP_SNAPSHOT, false, a, h->st)) return fail(PL_ERR_UNSUPPORTED, "snapshot kind");
+    if ((r = check_launch(h, 1))) return r;
+    if (host) {
+        double *buf;
+        if ((r = scratch(h, 2, &buf))) return r;
+        pl::launch_snap_to_node_major(h->snap[slot], h->np, h->n, h->q, buf, h->st);
+        if ((r = check_launch(h, 1))) return r;
+        return download(h, host, buf, (size_t)h->q * h->n);
+    }
+    return PL_OK;
+}
+
+int pl_residual(pl_lattice h, int family, double *out) {
+    if (!h || !out || family < 0 || family > 3) return fail(PL_ERR_ARG, "bad arguments");
+    double o[3];
+    int r = residual_family(h, family, o, true);
+    if (r) return r;
+    *out = o[2];
+    return PL_OK;
+}
+
+int pl_residual_host(pl_lattice h, int n, int ncomp, const double *const *a, const double *const *b, double *out) {
+    if (!h || !a || !b || !out || ncomp < 1 || ncomp > 3 || n < 1 || n > h->n * h->q / 6) return fail(PL_ERR_ARG, "bad arguments");
+    double *buf;
+    int r = scratch(h, 3, &buf);
+    if (r) return r;
+    pl::ResidArgs ra;
+    memset(&ra, 0, sizeof ra);
+    ra.ncomp = ncomp;
+    ra.n = n;
+    for (int m = 0; m < ncomp; ++m) {
+        double *da = buf + (size_t)(2 * m) * n, *db = buf + (size_t)(2 * m + 1) * n;
+        if ((r = upload(h, da, a[m], n)) || (r = upload(h, db, b[m], n))) return r;
+        ra.a[m] = da;
+        ra.b[m] = db;
+    }
+    CK(cudaMemsetAsync(h->nonfinite, 0, sizeof(int), h->st));
+    pl::launch_residual(ra, h->partial, pl::resid_blocks(n), h->nonfinite, h->dout, h->st);
+    if ((r = check_launch(h, 2))) return r;
+    double o[3];
+    if ((r = download(h, o, h->dout, 3))) return r;
+    *out = o[2];
+    return PL_OK;
+}
+
+int pl_sensitivity(pl_lattice h, int which, double *dfds, const double *dads, const double *dkds, const double *qn,
+                   const int *mask) {
+    if (!h || !dfds || !dads || which < 0 || which > 3) return fail(PL_ERR_ARG, "bad arguments");
+    if ((which <= 2 && !dkds) || (which == 0 && (!qn || !mask))) return fail(PL_ERR_ARG, "missing dkds / qn / mask");
+    if (h->adj_saved < 0) return fail(PL_ERR_STATE, "no saved adjoint collide");
+    if (which <= 1 && (!h->snap[0] || !h->snap[1])) return fail(PL_ERR_STATE, "take both snapshots (pl_snapshot) first");
+    for (int f = PL_FWD_RHO; f <= PL_FWD_TEM; ++f)
+        if (!h->fld[f]) return fail(PL_ERR_STATE, "forward solution not set (pl_freeze_forward)");
+    double *buf;
+    int r = scratch(h, 4, &buf);   // q*N >= 5*N
+    if (r) return r;
+    double *d_dfds = buf, *d_dads = buf + h->n, *d_dkds = buf + 2 * (size_t)h->n, *d_qn = buf + 3 * (size_t)h->n;
+    int *d_mask = reinterpret_cast<int *>(buf + 4 * (size_t)h->n);
+    if ((r = upload(h, d_dfds, dfds, h->n)) || (r = upload(h, d_dads, dads, h->n))) return r;
+    if (dkds && (r = upload(h, d_dkds, dkds, h->n))) return r;
+    if (qn && (r = upload(h, d_qn, qn, h->n))) return r;
+    if (mask) CK(cudaMemcpyAsync(d_mask, mask, sizeof(int) * h->n, cudaMemcpyHostToDevice, h->st));
+    if ((r = ensure_d(h, &h->fld[PL_KAPPA], h->n))) return r;
+    pl::SensArgs s;
+    memset(&s, 0, sizeof s);
+    s.which = which; s.n = h->n; s.nx = h->nx; s.ny = h->ny; s.nz = h->nz; s.np = h->np;
+    s.dfds = d_dfds; s.dads = d_dads; s.dkds = d_dkds; s.qn = d_qn; s.mask = d_mask;
+    s.ux = h->fld[PL_FWD_UX]; s.uy = h->fld[PL_FWD_UY]; s.uz = h->fld[PL_FWD_UZ]; s.tem = h->fld[PL_FWD_TEM];
+    const int sa = h->adj_saved;
+    s.imx = h->adj[sa][4]; s.imy = h->adj[sa][5]; s.imz = h->adj[sa][6];
+    s.item = h->adj[sa][7]; s.iqx = h->adj[sa][8]; s.iqy = h->adj[sa][9]; s.iqz = h->adj[sa][10];
+    s.kappa = h->fld[PL_KAPPA];
+    s.g = h->snap[0]; s.ig = h->snap[1];
+    pl::launch_sensitivity(h->q, s, h->st);
+    if ((r = check_launch(h, 1))) return r;
+    return download(h, dfds, d_dfds, h->n);
+}
+
+static int filter_common(pl_lattice h, int op, double R, double beta, const double *s, const double *d,
+                         const int *mask, double *out) {
+    if (!h || !s || !out || !(R > 0.0) || (op == 1 && !d)) return fail(PL_ERR_ARG, "bad arguments");
+    Taps *t = get_taps(h, R);
+    if (!t) return fail(PL_ERR_ALLOC, "filter taps");
+    double *buf;
+    int r = scratch(h, 5, &buf);
+    if (r) return r;
+    double *ds = buf, *dd = buf + h->n, *tmp = buf + 2 * (size_t)h->n, *dout = buf + 3 * (size_t)h->n;
+    int *dm = reinterpret_cast<int *>(buf + 4 * (size_t)h->n);
+    if ((r = upload(h, ds, s, h->n))) return r;
+    if (d && (r = upload(h, dd, d, h->n))) return r;
+    if (mask) CK(cudaMemcpyAsync(dm, mask, sizeof(int) * h->n, cudaMemcpyHostToDevice, h->st));
+    pl::FiltArgs f;
+    f.n = h->n; f.nx = h->nx; f.ny = h->ny; f.nz = h->nz; f.ntap = t->ntap;
+    f.di = t->di; f.dj = t->dj; f.dk = t->dk; f.hat = t->hat; f.mask = mask ? dm : nullptr; f.beta = beta;
+    pl::launch_filter(op, f, ds, dd, tmp, dout, h->st);
+    if ((r = check_launch(h, op == 1 ? 2 : 1))) return r;
+    return download(h, out, dout, h->n);
+}
+
+int pl_heaviside_var(pl_lattice h, double R, double beta, const double *s, const int *mask, double *out) {
+    return filter_common(h, 0, R, beta, s, nullptr, mask, out);
+}
+int pl_heaviside_sens(pl_lattice h, double R, double beta, const double *s, const double *dfdrho, const int *mask,
+                      double *out) {
+    return filter_common(h, 1, R, beta, s, dfdrho, mask, out);
+}
+int pl_density_filter(pl_lattice h, double R, const double *v, const int *mask, double *out) {
+    return filter_common(h, 2, R, 0.0, v, nullptr, mask, out);
+}
+
+int pl_normalize(pl_lattice h, double *v, int n) {
+    if (!h || !v || n < 1 || n > h->n * h->q) return fail(PL_ERR_ARG, "bad arguments");
+    double *buf;
+    int r = scratch(h, 6, &buf);
+    if (r) return r;
+    if ((r = upload(h, buf, v, n))) return r;
+    const int nblk = pl::resid_blocks(n);
+    pl::launch_normalize(buf, n, h->partial, nblk, h->st);
+    if ((r = check_launch(h, 2))) return r;
+    return download(h, v, buf, n);
+}
+
+int pl_stats(pl_lattice h, double *last_ms, long long *launches) {
+    if (!h) return fail(PL_ERR_ARG, "null handle");
+    if (last_ms) {
+        float ms = 0.f;
+        if (cudaEventQuery(h->ev1) == cudaSuccess && cudaEventElapsedTime(&ms, h->ev0, h->ev1) == cudaSuccess) h->last_ms = ms;
+        *last_ms = h->last_ms;
+    }
+    if (launches) *launches = h->launches;
+    return PL_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,300 @@
+// bc.cuh -- boundary-program ops applied to one node's populations (device code).
+//
+// Each op is one reference boundary routine restricted to one node of its edge/face:
+//   walls        D2Q9/D3Q15::(i)BoundaryConditionAlong* (d2q9.h:429-575, d3q15.h:982-1239)
+//   NS Zou-He    NS::BoundaryConditionSetU/SetRhoAlong* (navierstokes.h:90-426)
+//   AD           AD::BoundaryConditionSetT/SetQAlong* (advection.h:97-524)
+//   ANS adjoint  ANS::iBoundaryConditionSetU/SetRhoAlong* (adjointnavierstokes.h:95-392)
+//   AAD adjoint  AAD::iBoundaryConditionSetT/SetQ/SetRhoAlong* (adjointadvection.h:152-751)
+// The face of an op is (axis a, side d); "inward" populations have c_a == -d.
+#pragma once
+#include "physics.cuh"
+
+namespace pl {
+
+template <class L> __device__ __forceinline__ int cmp(int c, int a) { return comp<L>(c, a); }
+
+template <class L> __device__ __forceinline__ bool diag_of(int c, int a) {
+    bool r = false;
+#pragma unroll
+    for (int e = 0; e < L::ND; ++e) if (e != a && cmp<L>(c, e) != 0) r = true;
+    return r;
+}
+template <class L> __device__ __forceinline__ int opp_d(int c) { return opp<L>(c); }
+template <class L> __device__ __forceinline__ int refl_d(int c, int a) {
+    return a == 0 ? refl<L>(c, 0) : (a == 1 ? refl<L>(c, 1) : refl<L>(c, 2));
+}
+
+template <class L, class T> __device__ __forceinline__ T one_plus_3cu(int c, const T *u) {
+    T acc = T(1);
+#pragma unroll
+    for (int b = 0; b < L::ND; ++b) {
+        const int cb = cmp<L>(c, b);
+        if (cb > 0) acc += T(3) * u[b]; else if (cb < 0) acc -= T(3) * u[b];
+    }
+    return acc;
+}
+template <class L, class T> __device__ __forceinline__ T inv_w(int c) {
+    int s = 0;
+#pragma unroll
+    for (int b = 0; b < L::ND; ++b) s += abs(cmp<L>(c, b));
+    return s == 1 ? T(9) : (L::ND == 2 ? T(36) : T(72));
+}
+// sum over inward diagonals of sign(c_b) p_c, increasing c
+template <class L, class T> __device__ __forceinline__ T tsum(const T *p, int a, int d, int b) {
+    T s = T(0);
+#pragma unroll
+    for (int c = 1; c < L::Q; ++c) {
+        if (cmp<L>(c, a) != -d || !diag_of<L>(c, a)) continue;
+        const int cb = cmp<L>(c, b);
+        if (cb > 0) s += p[c]; else if (cb < 0) s -= p[c];
+    }
+    return s;
+}
+// kc * p_normal + sum of inward diagonals
+template <class L, class T> __device__ __forceinline__ T nsum(const T *p, int a, int d, T kc) {
+    T s = T(0);
+#pragma unroll
+    for (int c = 1; c < L::Q; ++c)
+        if (cmp<L>(c, a) == -d && !diag_of<L>(c, a)) s = kc * p[c];
+#pragma unroll
+    for (int c = 1; c < L::Q; ++c)
+        if (cmp<L>(c, a) == -d && diag_of<L>(c, a)) s += p[c];
+    return s;
+}
+__device__ __forceinline__ void tang3(int a, int &t0, int &t1) {
+    t0 = a == 0 ? 1 : (a == 1 ? 2 : 0);
+    t1 = a == 0 ? 2 : (a == 1 ? 0 : 1);
+}
+
+template <class L, class T>
+__device__ __noinline__ void apply_op(const Op &op, T *f, T *g, int node, const KArgs &a) {
+    const int A = op.axis, d = op.dir, nin = -d;
+    constexpr int Q = L::Q, ND = L::ND;
+    switch (op.kind) {
+    case BC_WALL:
+    case BC_IWALL: {
+        T *p = op.lat ? g : f;
+        const bool adj = op.kind == BC_IWALL;
+        T src[Q];
+#pragma unroll
+        for (int c = 0; c < Q; ++c) src[c] = p[c];
+#pragma unroll
+        for (int c = 1; c < Q; ++c) {
+            const int ca = cmp<L>(c, A);
+            if (adj ? (ca != d) : (ca != -d)) continue;
+            p[c] = op.sub == 1 ? src[opp_d<L>(c)] : src[refl_d<L>(c, A)];
+        }
+        break;
+    }
+    case BC_NS_U:
+    case BC_NS_RHO: {
+        T *p = f;
+        T u[3] = {T(0), T(0), T(0)};
+        T sT = T(0), sO = T(0);
+        bool first = true;
+#pragma unroll
+        for (int c = 0; c < Q; ++c)
+            if (cmp<L>(c, A) == 0) { if (first) { sT = p[c]; first = false; } else sT += p[c]; }
+        first = true;
+#pragma unroll
+        for (int c = 0; c < Q; ++c)
+            if (cmp<L>(c, A) == d) { if (first) { sO = p[c]; first = false; } else sO += p[c]; }
+        const T S = sT + T(2) * sO;
+        T rho0;
+        if (op.kind == BC_NS_U) {
+            u[0] = T(op.v0); u[1] = T(op.v1); if (ND == 3) u[2] = T(op.v2);
+            rho0 = S / (d < 0 ? T(1) - u[A] : T(1) + u[A]);
+        } else {
+            rho0 = T(op.v0);
+            if (ND == 2) u[1 - A] = T(op.v1);
+            else { u[(A + 1) % 3] = T(op.v1); u[(A + 2) % 3] = T(op.v2); }
+            u[A] = d < 0 ? T(1) - S / rho0 : T(-1) + S / rho0;
+        }
+        const T kn = ND == 2 ? T(6) : T(12), kt = ND == 2 ? T(0.5) : T(0.25), kc = ND == 2 ? T(4) : T(8);
+        T m[3];
+#pragma unroll
+        for (int b = 0; b < ND; ++b) {
+            if (b == A) m[b] = rho0 * u[b] / kn;
+            else {
+                T fp = T(0), fm = T(0);
+#pragma unroll
+                for (int c = 1; c < Q; ++c) {
+                    if (diag_of<L>(c, b)) continue;
+                    if (cmp<L>(c, b) == 1) fp = p[c];
+                    if (cmp<L>(c, b) == -1) fm = p[c];
+                }
+                m[b] = kt * (fp - fm - rho0 * u[b]);
+            }
+        }
+        T src[Q];
+#pragma unroll
+        for (int c = 0; c < Q; ++c) src[c] = p[c];
+#pragma unroll
+        for (int c = 1; c < Q; ++c) {
+            if (cmp<L>(c, A) != -d) continue;
+            T v = src[opp_d<L>(c)];
+            if (!diag_of<L>(c, A)) {
+                v = cmp<L>(c, A) > 0 ? v + kc * m[A] : v - kc * m[A];
+            } else {
+#pragma unroll
+                for (int b = 0; b < ND; ++b) {
+                    const int cb = cmp<L>(c, b);
+                    if (b == A) v = cb > 0 ? v + m[b] : v - m[b];
+                    else v = cb > 0 ? v - m[b] : v + m[b];
+                }
+            }
+            p[c] = v;
+        }
+        break;
+    }
+    case BC_AD_T:
+    case BC_AD_Q:
+    case BC_AD_QC: {
+        T *p = g;
+        const T u[3] = {T(a.bcu[0][node]), T(a.bcu[1][node]), ND == 3 ? T(a.bcu[2][node]) : T(0)};
+        T tem0;
+        if (op.kind == BC_AD_T) {
+            T s = T(op.v0);
+#pragma unroll
+            for (int c = 0; c < Q; ++c) if (cmp<L>(c, A) != -d) s -= p[c];
+            tem0 = T(6) * s / (nin > 0 ? T(1) + T(3) * u[A] : T(1) - T(3) * u[A]);
+        } else {
+            const T kap = op.kind == BC_AD_Q ? T(a.bckappa[node]) : T(op.v1);
+            T s = (T(1) + T(1) / (T(6) * kap)) * T(op.v0);
+#pragma unroll
+            for (int c = 1; c < Q; ++c) if (cmp<L>(c, A) == d) s += p[c];
+            tem0 = T(6) * s / (nin > 0 ? T(1) - T(3) * u[A] : T(1) + T(3) * u[A]);
+        }
+#pragma unroll
+        for (int c = 1; c < Q; ++c)
+            if (cmp<L>(c, A) == -d) p[c] = tem0 * one_plus_3cu<L, T>(c, u) / inv_w<L, T>(c);
+        break;
+    }
+    case BC_ANS_U:
+    case BC_ANS_RHO: {
+        T *p = f;
+        T rho0;
+        if (op.kind == BC_ANS_RHO) {
+            rho0 = nsum<L, T>(p, A, d, ND == 2 ? T(4) : T(8)) / (ND == 2 ? T(3) : T(6));
+            T src[Q];
+#pragma unroll
+            for (int c = 0; c < Q; ++c) src[c] = p[c];
+#pragma unroll
+            for (int c = 1; c < Q; ++c) if (cmp<L>(c, A) == d) p[c] = src[opp_d<L>(c)] - rho0;
+            break;
+        }
+        const T u[3] = {T(op.v0), T(op.v1), ND == 3 ? T(op.v2) : T(0)};
+        if (ND == 2) {
+            const T un = u[0], ut = A == 0 ? u[1] : u[0];   // y edges use ux twice (reference)
+            const int b = 1 - A;
+            const T ns = nsum<L, T>(p, A, d, T(4));
+            const T ts = tsum<L, T>(p, A, d, b);
+            T num = d < 0 ? T(-2) * T(op.eps) + un * ns : T(-2) * T(op.eps) - un * ns;
+            num += T(3) * ut * ts;
+            rho0 = num / (T(3) * (d < 0 ? T(1) - un : T(1) + un));
+        } else {
+            T num = T(-4) * T(op.eps);
+#pragma unroll
+            for (int b = 0; b < 3; ++b) {
+                if (b == A) {
+                    const T ns = nsum<L, T>(p, A, d, T(8));
+                    num = d < 0 ? num + u[A] * ns : num - u[A] * ns;
+                } else {
+                    num += T(3) * u[b] * tsum<L, T>(p, A, d, b);
+                }
+            }
+            rho0 = num / (T(6) * (d < 0 ? T(1) - u[A] : T(1) + u[A]));
+        }
+        T src[Q];
+#pragma unroll
+        for (int c = 0; c < Q; ++c) src[c] = p[c];
+#pragma unroll
+        for (int c = 1; c < Q; ++c) if (cmp<L>(c, A) == d) p[c] = src[opp_d<L>(c)] + rho0;
+        break;
+    }
+    case BC_AAD_T:
+    case BC_AAD_Q: {
+        T *p = g;
+        const T u[3] = {T(a.bcu[0][node]), T(a.bcu[1][node]), ND == 3 ? T(a.bcu[2][node]) : T(0)};
+        const T pre = nin > 0 ? T(1) + T(3) * u[A] : T(1) - T(3) * u[A];
+        const T post = nin > 0 ? T(1) - T(3) * u[A] : T(1) + T(3) * u[A];
+        T rho0;
+        if (op.kind == BC_AAD_T) {
+            if (ND == 2) {
+                T num = T(0);
+#pragma unroll
+                for (int c = 1; c < Q; ++c)
+                    if (cmp<L>(c, A) == -d && !diag_of<L>(c, A)) num = T(4) * one_plus_3cu<L, T>(c, u) * p[c];
+#pragma unroll
+                for (int c = 1; c < Q; ++c)
+                    if (cmp<L>(c, A) == -d && diag_of<L>(c, A)) num += one_plus_3cu<L, T>(c, u) * p[c];
+                rho0 = -num / (T(6) * pre);
+            } else {
+                int t0, t1;
+                tang3(A, t0, t1);
+                rho0 = -nsum<L, T>(p, A, d, T(8)) / T(12) - u[t0] * tsum<L, T>(p, A, d, t0) / (T(4) * pre)
+                       - u[t1] * tsum<L, T>(p, A, d, t1) / (T(4) * pre);
+            }
+        } else {
+            if (ND == 2) {
+                const int b = 1 - A;
+                const T num = pre * nsum<L, T>(p, A, d, T(4)) + T(3) * u[b] * tsum<L, T>(p, A, d, b) - T(12) * T(op.eps);
+                rho0 = num / (T(6) * post);
+            } else {
+                int t0, t1;
+                tang3(A, t0, t1);
+                const bool k3 = (A == 0 || (A == 1 && d < 0));   // reference factor pattern
+                T num = pre * nsum<L, T>(p, A, d, T(8));
+                if (k3) {
+                    num += T(3) * u[t0] * tsum<L, T>(p, A, d, t0);
+                    num += T(3) * u[t1] * tsum<L, T>(p, A, d, t1);
+                } else {
+                    num += u[t0] * tsum<L, T>(p, A, d, t0);
+                    num += u[t1] * tsum<L, T>(p, A, d, t1);
+                }
+                num -= T(24) * T(op.eps);
+                rho0 = num / (T(12) * post);
+            }
+        }
+#pragma unroll
+        for (int c = 1; c < Q; ++c) if (cmp<L>(c, A) == d) p[c] = rho0;
+        break;
+    }
+    case BC_AAD_RHO: {
+        const T u[3] = {T(a.bcu[0][node]), T(a.bcu[1][node]), ND == 3 ? T(a.bcu[2][node]) : T(0)};
+        const T rho = T(a.bcrho[node]), tem = T(a.bctem[node]);
+        const T pre = nin > 0 ? T(1) + T(3) * u[A] : T(1) - T(3) * u[A];
+        const T post = nin > 0 ? T(1) - T(3) * u[A] : T(1) + T(3) * u[A];
+        T r0, flux0 = T(0);
+        const int type = op.sub;
+        if (ND == 2) {
+            const int b = 1 - A;
+            r0 = -nsum<L, T>(f, A, d, T(4)) / T(3);
+            if (type == 1) flux0 = tem * u[b] * tsum<L, T>(g, A, d, b) / (T(2) * pre * rho);
+            else if (type == 2)
+                flux0 = -tem * (nsum<L, T>(g, A, d, T(4)) / T(3) + u[b] * tsum<L, T>(g, A, d, b) / T(2)) / (post * rho);
+        } else {
+            int t0, t1;
+            tang3(A, t0, t1);
+            r0 = -nsum<L, T>(f, A, d, T(8)) / T(6);
+            const T tt = u[t0] * tsum<L, T>(g, A, d, t0) / T(4) + u[t1] * tsum<L, T>(g, A, d, t1) / T(4);
+            if (type == 1) flux0 = tem * tt / (rho * pre);
+            else if (type == 2)
+                flux0 = -tem * (nsum<L, T>(g, A, d, T(8)) / T(6) + u[t0] * tsum<L, T>(g, A, d, t0) / T(4)
+                                + u[t1] * tsum<L, T>(g, A, d, t1) / T(4)) / (rho * post);
+        }
+        const T obj0 = T(op.eps) * T(2) * tem / (post * rho);
+        T src[Q];
+#pragma unroll
+        for (int c = 0; c < Q; ++c) src[c] = f[c];
+#pragma unroll
+        for (int c = 1; c < Q; ++c) if (cmp<L>(c, A) == d) f[c] = src[opp_d<L>(c)] + r0 + flux0 + obj0;
+        break;
+    }
+    default:
+        break;
+    }
+}
+
+}  // namespace pl

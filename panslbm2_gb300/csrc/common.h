@@ -1,0 +1,78 @@
+// common.h -- host/device shared descriptors of the CUDA library.
+#pragma once
+#include <stdint.h>
+
+namespace pl {
+
+// Collide kinds (one per reference collide routine; see include/panslbm_gb300.h).
+enum Kind {
+    K_NS_COLLIDE = 0, K_NS_BRINKMAN = 1, K_AD_NATURAL = 2, K_AD_FORCE = 3, K_AD_HEATEX = 4,
+    K_AD_NATURAL_NOBRINK = 5, K_AD_FORCE_NOBRINK = 6,
+    K_ANS_BRINKMAN = 10, K_AAD_NATURAL = 11, K_AAD_FORCE = 12, K_AAD_HEATEX = 13, K_AAD_MASSFLOW = 14
+};
+__host__ __device__ constexpr bool kind_is_adjoint(int k) { return k >= 10; }
+__host__ __device__ constexpr bool kind_has_g(int k) { return !(k == K_NS_COLLIDE || k == K_NS_BRINKMAN || k == K_ANS_BRINKMAN); }
+__host__ __device__ constexpr bool kind_node_kappa(int k) {
+    return k == K_AD_NATURAL || k == K_AD_FORCE || k == K_AAD_NATURAL || k == K_AAD_FORCE || k == K_AAD_MASSFLOW;
+}
+__host__ __device__ constexpr bool kind_has_snapshot(int k) {
+    return k == K_AD_NATURAL || k == K_AD_FORCE || k == K_AAD_NATURAL || k == K_AAD_FORCE || k == K_AAD_MASSFLOW;
+}
+
+// Boundary-program op kinds (same numbering as the oracle) plus smoothing.
+enum BcKind {
+    BC_WALL = 0, BC_IWALL = 1, BC_NS_U = 2, BC_NS_RHO = 3, BC_AD_T = 4, BC_AD_Q = 5, BC_AD_QC = 6,
+    BC_ANS_U = 7, BC_ANS_RHO = 8, BC_AAD_T = 9, BC_AAD_Q = 10, BC_AAD_RHO = 11, BC_SMOOTH = 20
+};
+
+// One boundary-program op as applied at one node. `lat` selects the population set the op
+// writes (0 = NS set f, 1 = AD set g). For BC_SMOOTH, nnbr neighbours are averaged.
+struct Op {
+    int32_t kind;
+    int8_t axis, dir, lat, sub;   // sub: wall type (1 BARRIER, 2 MIRROR) / iSetRho type / nnbr
+    int32_t seq;                  // position in the recorded call order
+    int32_t node;                 // node the op writes (differs from the owner for the
+                                  // D3Q15 +x MIRROR quirk)
+    int32_t nbr[3];
+    double v0, v1, v2, eps;
+};
+
+struct Geo {
+    int nx, ny, nz, n;    // lattice extents, node count
+    long long np;         // plane stride of one population (n rounded up)
+    uint32_t face_mask;   // bit a*2+s: face (axis a, side s) carries boundary ops
+    const uint8_t *flags; // optional per-node "has boundary ops" flags (interior lines)
+};
+
+struct Phys { double nu, diff, gx, gy, gz, tem0, shift_f, shift_g; };
+
+// Arguments of every population kernel. Field pointers are device pointers; `T*` members are
+// stored as void* and cast to the kernel's compute type.
+struct KArgs {
+    Geo geo;
+    const void *src;            // populations read (f planes then g planes)
+    void *dst;                  // populations written
+    const void *alpha, *kappa, *beta, *dirx, *diry, *dirz;   // design fields, compute type
+    const void *fwd[5];         // adjoint kinds: forward rho, ux, uy, uz, tem (compute type)
+    double *out[11];            // macro outputs (forward: rho,ux,uy,uz,tem,qx,qy,qz;
+                                //  adjoint: ip,iux,iuy,iuz,imx,imy,imz,item,iqx,iqy,iqz)
+    double *snap;               // pre-collision g snapshot, [q][np] planes
+    // boundary program
+    const int *bnode;           // boundary nodes (sorted)
+    const int *bstart;          // CSR op offsets per boundary node
+    const Op *ops;
+    const int *slot_of;         // node -> boundary slot or -1
+    int nb;
+    const double *bcu[3];       // velocity read by AD / AAD boundary ops
+    const double *bcrho, *bctem;  // forward rho / T read by AAD iSetRho
+    const double *bckappa;      // per-node kappa read by AD SetQ
+    double *bcu_out[3];         // where this step stores the new velocity of boundary nodes
+    Phys ph;
+    int pull;                   // 1: stream (pull) before the boundary program
+    int save;                   // 1: write macro outputs
+    int *err;                   // device error word (bit flags)
+};
+
+enum ErrBits { ERR_RECURSION = 1, ERR_BAD_OP = 2 };
+
+}  // namespace pl

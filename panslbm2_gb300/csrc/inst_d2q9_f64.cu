@@ -1,0 +1,6 @@
+// Kernel instantiations for D2Q9 with double population storage.
+#define PL_LAT D2Q9
+#define PL_STORE double
+#define PL_NAME d2q9_f64
+#define PL_ALL_KINDS
+#include "inst_body.cuh"

@@ -1,0 +1,6 @@
+// Kernel instantiations for D3Q15 with double population storage.
+#define PL_LAT D3Q15
+#define PL_STORE double
+#define PL_NAME d3q15_f64
+#define PL_ALL_KINDS
+#include "inst_body.cuh"

@@ -1,0 +1,230 @@
+// kernels.cuh -- population kernels of the fused lattice-Boltzmann step.
+//
+// One time step of the reference loop is  collide -> Stream -> boundary routines -> smoothing
+// (e.g. production/heatsink.cpp:142-174). Here the step is regrouped as
+//     pull-stream + boundary program + collide      (one pass over HBM per step)
+// split into an interior kernel (every node without boundary ops: pull, collide, store) and a
+// boundary kernel (nodes with ops: pull, replay the recorded ops in call order -- recursing
+// into neighbours for the averaging of SmoothCorner* -- then the same collide).
+// Populations are structure-of-arrays: plane c of set s at  buf + (s*Q + c)*np.
+#pragma once
+#include "bc.cuh"
+
+namespace pl {
+
+constexpr int kBlock = 256;
+
+template <class L> __device__ __forceinline__ void coords(const Geo &g, int idx, int &i, int &j, int &k) {
+    i = idx % g.nx;
+    const int r = idx / g.nx;
+    if (L::ND == 2) { j = r; k = 0; }
+    else { j = r % g.ny; k = r / g.ny; }
+}
+template <class L> __device__ __forceinline__ bool is_interior(const Geo &g, int i, int j, int k) {
+    return i > 0 && i < g.nx - 1 && j > 0 && j < g.ny - 1 && (L::ND == 2 || (k > 0 && k < g.nz - 1));
+}
+template <class L> __device__ __forceinline__ bool skip_boundary(const Geo &g, int idx, int i, int j, int k) {
+    if (g.flags) return g.flags[idx] != 0;
+    const uint32_t m = g.face_mask;
+    return ((m & 1u) && i == 0) || ((m & 2u) && i == g.nx - 1) || ((m & 4u) && j == 0) ||
+           ((m & 8u) && j == g.ny - 1) || (L::ND == 3 && (((m & 16u) && k == 0) || ((m & 32u) && k == g.nz - 1)));
+}
+__device__ __forceinline__ int wrap1(int i, int n) { return i < 0 ? n - 1 : (i >= n ? 0 : i); }
+
+// Load one node's populations from `src`, pulled along direction sgn*c (sgn = -1: Stream,
+// +1: iStream) when `pull`, else in place. Periodic single-step wrap (d2q9.h:80-84).
+template <class L, class S, bool HAS_G>
+__device__ __forceinline__ void load_node(const S *__restrict__ src, const Geo &g, int idx, int i, int j, int k,
+                                          bool pull, int sgn, bool interior, typename Store<S>::T *f,
+                                          typename Store<S>::T *gg, typename Store<S>::T sf,
+                                          typename Store<S>::T sg) {
+    using T = typename Store<S>::T;
+    constexpr int Q = L::Q;
+    const long long np = g.np;
+#pragma unroll
+    for (int c = 0; c < Q; ++c) {
+        int s = idx;
+        if (pull && c > 0) {
+            const int dx = sgn * L::cx(c), dy = sgn * L::cy(c), dz = sgn * L::cz(c);
+            if (interior) s = idx + dx + g.nx * (dy + g.ny * dz);
+            else s = wrap1(i + dx, g.nx) + g.nx * (wrap1(j + dy, g.ny) + g.ny * (L::ND == 3 ? wrap1(k + dz, g.nz) : 0));
+        }
+        f[c] = Store<S>::dec(Store<S>::ld(src + (long long)c * np + s), L::template w<T>(c) * sf);
+        if (HAS_G) gg[c] = Store<S>::dec(Store<S>::ld(src + (long long)(Q + c) * np + s), L::template w<T>(c) * sg);
+    }
+}
+template <class L, class S, bool HAS_G>
+__device__ __forceinline__ void store_node(S *__restrict__ dst, const Geo &g, int idx, const typename Store<S>::T *f,
+                                           const typename Store<S>::T *gg, typename Store<S>::T sf,
+                                           typename Store<S>::T sg) {
+    using T = typename Store<S>::T;
+    constexpr int Q = L::Q;
+#pragma unroll
+    for (int c = 0; c < Q; ++c) {
+        Store<S>::st(dst + (long long)c * g.np + idx, Store<S>::enc(f[c], L::template w<T>(c) * sf));
+        if (HAS_G) Store<S>::st(dst + (long long)(Q + c) * g.np + idx, Store<S>::enc(gg[c], L::template w<T>(c) * sg));
+    }
+}
+
+// ---- interior kernel --------------------------------------------------------------------
+template <class L, class S, int K, bool SAVE, bool PULL>
+__global__ void __launch_bounds__(kBlock) k_interior(KArgs a) {
+    using T = typename Store<S>::T;
+    constexpr bool HG = kind_has_g(K);
+    const int idx = blockIdx.x * kBlock + threadIdx.x;
+    if (idx >= a.geo.n) return;
+    int i, j, k;
+    coords<L>(a.geo, idx, i, j, k);
+    if (PULL && skip_boundary<L>(a.geo, idx, i, j, k)) return;
+    T f[L::Q], g[L::Q];
+    const T sf = T(a.ph.shift_f), sg = T(a.ph.shift_g);
+    load_node<L, S, HG>(static_cast<const S *>(a.src), a.geo, idx, i, j, k, PULL, K >= 10 ? 1 : -1,
+                        is_interior<L>(a.geo, i, j, k), f, g, sf, sg);
+    collide_node<L, T, K>(f, g, idx, a, SAVE, nullptr, a.geo.np, nullptr);
+    store_node<L, S, HG>(static_cast<S *>(a.dst), a.geo, idx, f, g, sf, sg);
+}
+
+// ---- boundary program replay ----------------------------------------------------------------
+// State of `node` after every op recorded before `seq_limit` (the reference applies edge
+// routines in call order; SmoothCorner* reads neighbours as they stand at that point).
+template <class L, class S, int D>
+__device__ __noinline__ void eval_node(const KArgs &a, int node, int seq_limit, typename Store<S>::T *f, typename Store<S>::T *g,
+                          bool has_g, int sgn) {
+    using T = typename Store<S>::T;
+    constexpr int Q = L::Q;
+    int i, j, k;
+    coords<L>(a.geo, node, i, j, k);
+    const T sf = T(a.ph.shift_f), sg = T(a.ph.shift_g);
+    if (has_g) load_node<L, S, true>(static_cast<const S *>(a.src), a.geo, node, i, j, k, a.pull != 0, sgn,
+                                     is_interior<L>(a.geo, i, j, k), f, g, sf, sg);
+    else load_node<L, S, false>(static_cast<const S *>(a.src), a.geo, node, i, j, k, a.pull != 0, sgn,
+                                is_interior<L>(a.geo, i, j, k), f, g, sf, sg);
+    const int slot = a.slot_of[node];
+    if (slot < 0) return;
+    const int o1 = a.bstart[slot + 1];
+    for (int o = a.bstart[slot]; o < o1; ++o) {
+        const Op op = a.ops[o];
+        if (op.seq >= seq_limit) break;
+        if (op.kind == BC_SMOOTH) {
+            if constexpr (D == 0) {
+                atomicOr(a.err, ERR_RECURSION);   // chain deeper than any reference smoothing sequence
+            } else {
+                T acc[Q];
+                const int nn = op.sub;
+                for (int m = 0; m < nn; ++m) {
+                    T fn[Q], gn[Q];
+                    eval_node<L, S, D - 1>(a, op.nbr[m], op.seq, fn, gn, has_g, sgn);
+                    const T *p = op.lat ? gn : fn;
+#pragma unroll
+                    for (int c = 0; c < Q; ++c) acc[c] = m == 0 ? p[c] : acc[c] + p[c];
+                }
+                T *p = op.lat ? g : f;
+#pragma unroll
+                for (int c = 0; c < Q; ++c) p[c] = nn == 2 ? T(0.5) * acc[c] : acc[c] / T(3);
+            }
+        } else {
+            apply_op<L, T>(op, f, g, node, a);
+        }
+    }
+}
+
+template <class L, class S, int K>
+__global__ void __launch_bounds__(128) k_boundary(KArgs a) {
+    using T = typename Store<S>::T;
+    constexpr bool HG = kind_has_g(K);
+    const int s = blockIdx.x * 128 + threadIdx.x;
+    if (s >= a.nb) return;
+    const int idx = a.bnode[s];
+    T f[L::Q], g[L::Q];
+    eval_node<L, S, 4>(a, idx, 0x7fffffff, f, g, HG, K >= 10 ? 1 : -1);
+    T u[3];
+    collide_node<L, T, K>(f, g, idx, a, a.save != 0, nullptr, a.geo.np, K < 10 ? u : nullptr);
+    if (K < 10 && a.bcu_out[0]) {
+        a.bcu_out[0][idx] = double(u[0]);
+        a.bcu_out[1][idx] = double(u[1]);
+        if (L::ND == 3) a.bcu_out[2][idx] = double(u[2]);
+    }
+    const T sf = T(a.ph.shift_f), sg = T(a.ph.shift_g);
+    store_node<L, S, HG>(static_cast<S *>(a.dst), a.geo, idx, f, g, sf, sg);
+}
+
+// ---- snapshot: the collide's pre-relaxation g (what the reference stores in gi / igi) ----
+template <class L, class S, int K>
+__global__ void __launch_bounds__(128) k_snapshot(KArgs a) {
+    using T = typename Store<S>::T;
+    const int idx = blockIdx.x * 128 + threadIdx.x;
+    if (idx >= a.geo.n) return;
+    T f[L::Q], g[L::Q];
+    eval_node<L, S, 4>(a, idx, 0x7fffffff, f, g, true, K >= 10 ? 1 : -1);
+    collide_node<L, T, K>(f, g, idx, a, false, a.snap, a.geo.np, nullptr);
+}
+
+// ---- stream + boundary program without collide (pre-collision state to dst) ----------------
+template <class L, class S>
+__global__ void __launch_bounds__(128) k_stream_program(KArgs a, int has_g, int sgn) {
+    using T = typename Store<S>::T;
+    const int idx = blockIdx.x * 128 + threadIdx.x;
+    if (idx >= a.geo.n) return;
+    T f[L::Q], g[L::Q];
+    eval_node<L, S, 4>(a, idx, 0x7fffffff, f, g, has_g != 0, sgn);
+    const T sf = T(a.ph.shift_f), sg = T(a.ph.shift_g);
+    if (has_g) store_node<L, S, true>(static_cast<S *>(a.dst), a.geo, idx, f, g, sf, sg);
+    else store_node<L, S, false>(static_cast<S *>(a.dst), a.geo, idx, f, g, sf, sg);
+}
+
+// ---- equilibrium initial conditions (navierstokes.h:548-572, advection.h:1046-1070,
+//      adjointnavierstokes.h:472-498, adjointadvection.h:1357-1381) ---------------------------
+// which: 0 NS (rho,u), 1 AD (T,u), 2 ANS (ip,iu; u), 3 AAD (iT,iq; u). in[]: double fields.
+template <class L, class S>
+__global__ void k_init(KArgs a, int which, const double *in0, const double *in1, const double *in2,
+                       const double *in3, const double *ux, const double *uy, const double *uz) {
+    using T = typename Store<S>::T;
+    const int idx = blockIdx.x * kBlock + threadIdx.x;
+    if (idx >= a.geo.n) return;
+    constexpr int Q = L::Q;
+    const T u[3] = {T(ux[idx]), T(uy[idx]), L::ND == 3 ? T(uz[idx]) : T(0)};
+    S *dst = static_cast<S *>(a.dst);
+    const int set = (which == 1 || which == 3) ? 1 : 0;
+    const T sh = set ? T(a.ph.shift_g) : T(a.ph.shift_f);
+    T eq[Q];
+    if (which == 0) {
+        const T uu = ns_uu<L, T>(u);
+#pragma unroll
+        for (int c = 0; c < Q; ++c) eq[c] = ns_feq<L, T>(c, T(in0[idx]), u, uu);
+    } else if (which == 1) {
+#pragma unroll
+        for (int c = 0; c < Q; ++c) eq[c] = ad_geq<L, T>(c, T(in0[idx]), u);
+    } else if (which == 2) {
+        const T iu[3] = {T(in1[idx]), T(in2[idx]), L::ND == 3 ? T(in3[idx]) : T(0)};
+#pragma unroll
+        for (int c = 0; c < Q; ++c) eq[c] = ans_feq<L, T>(c, u, T(in0[idx]), iu);
+    } else {
+        const T iq[3] = {T(in1[idx]), T(in2[idx]), L::ND == 3 ? T(in3[idx]) : T(0)};
+        const T v = T(in0[idx]) + T(3) * vdot<L, T>(u, iq);
+#pragma unroll
+        for (int c = 0; c < Q; ++c) eq[c] = v;
+    }
+#pragma unroll
+    for (int c = 0; c < Q; ++c)
+        Store<S>::st(dst + (long long)(set * Q + c) * a.geo.np + idx, Store<S>::enc(eq[c], L::template w<T>(c) * sh));
+}
+
+// population transfer between the storage format and double SoA (host exchange)
+template <class L, class S>
+__global__ void k_decode(const S *src, double *out, long long np, int n, int set, double shift) {
+    using T = typename Store<S>::T;
+    const long long t = (long long)blockIdx.x * kBlock + threadIdx.x;
+    if (t >= (long long)L::Q * n) return;
+    const int c = int(t / n), idx = int(t % n);
+    out[t] = double(Store<S>::dec(src[(long long)(set * L::Q + c) * np + idx], L::template w<T>(c) * T(shift)));
+}
+template <class L, class S>
+__global__ void k_encode(const double *in, S *dst, long long np, int n, int set, double shift) {
+    using T = typename Store<S>::T;
+    const long long t = (long long)blockIdx.x * kBlock + threadIdx.x;
+    if (t >= (long long)L::Q * n) return;
+    const int c = int(t / n), idx = int(t % n);
+    dst[(long long)(set * L::Q + c) * np + idx] = Store<S>::enc(T(in[t]), L::template w<T>(c) * T(shift));
+}
+
+}  // namespace pl

@@ -1,0 +1,23 @@
+// launch.h -- host-side declarations of the per-(lattice, storage) launch switches.
+#pragma once
+#include <cuda_runtime.h>
+#include "common.h"
+
+namespace pl {
+enum LaunchOp { OP_COLLIDE = 0, OP_STEP = 1, OP_BOUNDARY = 2, OP_SNAPSHOT = 3 };
+enum AuxOp { AUX_STREAM_PROGRAM = 0, AUX_INIT = 1, AUX_DECODE = 2, AUX_ENCODE = 3 };
+
+#define PL_DECL(name)                                                                                   \
+    int launch_##name(int kind, int op, bool save, const KArgs &a, cudaStream_t st);                     \
+    void aux_##name(int op, const KArgs &a, int which, const double *const *in, int has_g, int sgn,     \
+                    double *buf, int set, double shift, cudaStream_t st);
+PL_DECL(d2q9_f64)
+PL_DECL(d2q9_f32)
+PL_DECL(d2q9_f16)
+PL_DECL(d2q9_bf16)
+PL_DECL(d3q15_f64)
+PL_DECL(d3q15_f32)
+PL_DECL(d3q15_f16)
+PL_DECL(d3q15_bf16)
+#undef PL_DECL
+}  // namespace pl

@@ -1,0 +1,312 @@
+// physics.cuh -- per-node lattice-Boltzmann arithmetic of the NS / AD forward and adjoint
+// collides (device code). Each routine restates the reference routine cited beside it with
+// the same evaluation order, so FP64 builds compiled without FMA contraction reproduce the
+// reference's scalar results; FP32 builds are the throughput path.
+#pragma once
+#include "common.h"
+#include "lattice.cuh"
+
+namespace pl {
+
+// c . u over the non-zero components of c, left to right (x, y, z)
+template <class L, class T> __device__ __forceinline__ T cdot(int c, T u0, T u1, T u2) {
+    T s = T(0);
+    bool first = true;
+    const int a0 = L::cx(c), a1 = L::cy(c), a2 = L::cz(c);
+    if (a0 != 0) { s = a0 > 0 ? u0 : -u0; first = false; }
+    if (a1 != 0) { if (first) { s = a1 > 0 ? u1 : -u1; first = false; } else s = a1 > 0 ? s + u1 : s - u1; }
+    if (L::ND == 3 && a2 != 0) { if (first) { s = a2 > 0 ? u2 : -u2; } else s = a2 > 0 ? s + u2 : s - u2; }
+    return s;
+}
+template <class L, class T> __device__ __forceinline__ T vdot(const T *a, const T *b) {
+    return L::ND == 2 ? a[0] * b[0] + a[1] * b[1] : a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
+}
+template <class L, class T> __device__ __forceinline__ T wt(int c) { return L::template w<T>(c); }
+
+// NS::Macro (navierstokes.h:15-50)
+template <class L, class T> __device__ __forceinline__ void ns_macro(const T *f, T &rho, T *u) {
+    T r = f[0], m0 = T(0), m1 = T(0), m2 = T(0);
+#pragma unroll
+    for (int c = 1; c < L::Q; ++c) {
+        const T v = f[c];
+        r += v;
+        if (L::cx(c) == 1) m0 += v; else if (L::cx(c) == -1) m0 -= v;
+        if (L::cy(c) == 1) m1 += v; else if (L::cy(c) == -1) m1 -= v;
+        if (L::cz(c) == 1) m2 += v; else if (L::cz(c) == -1) m2 -= v;
+    }
+    const T inv = T(1) / r;
+    rho = r;
+    u[0] = m0 * inv;
+    u[1] = m1 * inv;
+    u[2] = L::ND == 3 ? m2 * inv : T(0);
+}
+// NS::Equilibrium (navierstokes.h:52-70), fused into the BGK relaxation
+template <class L, class T> __device__ __forceinline__ T ns_feq(int c, T rho, const T *u, T uu) {
+    const T ciu = cdot<L, T>(c, u[0], u[1], u[2]);
+    return wt<L, T>(c) * rho * (T(3) * ciu + T(4.5) * ciu * ciu + uu);
+}
+template <class L, class T> __device__ __forceinline__ T ns_uu(const T *u) {
+    return L::ND == 2 ? T(1) - T(1.5) * (u[0] * u[0] + u[1] * u[1])
+                      : T(1) - T(1.5) * (u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
+}
+// NS::ExternalForceBrinkman (navierstokes.h:72-88)
+template <class L, class T> __device__ __forceinline__ void ns_brinkman(T *f, T rho, const T *u, T alpha) {
+    const T coef = T(3) * alpha * rho / (rho + alpha);
+#pragma unroll
+    for (int c = 1; c < L::Q; ++c) f[c] -= coef * wt<L, T>(c) * cdot<L, T>(c, u[0], u[1], u[2]);
+}
+// AD::Macro (advection.h:16-51)
+template <class L, class T> __device__ __forceinline__ void ad_macro(const T *g, const T *u, T omg, T &tem, T *q) {
+    T t = g[0], s0 = T(0), s1 = T(0), s2 = T(0);
+#pragma unroll
+    for (int c = 1; c < L::Q; ++c) {
+        const T v = g[c];
+        t += v;
+        if (L::cx(c) == 1) s0 += v; else if (L::cx(c) == -1) s0 -= v;
+        if (L::cy(c) == 1) s1 += v; else if (L::cy(c) == -1) s1 -= v;
+        if (L::cz(c) == 1) s2 += v; else if (L::cz(c) == -1) s2 -= v;
+    }
+    const T coef = T(1) - T(0.5) * omg;
+    tem = t;
+    q[0] = coef * (s0 - t * u[0]);
+    q[1] = coef * (s1 - t * u[1]);
+    q[2] = L::ND == 3 ? coef * (s2 - t * u[2]) : T(0);
+}
+// AD::Equilibrium (advection.h:53-69)
+template <class L, class T> __device__ __forceinline__ T ad_geq(int c, T tem, const T *u) {
+    return wt<L, T>(c) * tem * (T(1) + T(3) * cdot<L, T>(c, u[0], u[1], u[2]));
+}
+// AD::ExternalForceNaturalConvection (advection.h:71-85)
+template <class L, class T> __device__ __forceinline__ void ad_nc_force(T *f, T tem, T gx, T gy, T gz, T tem0) {
+#pragma unroll
+    for (int c = 1; c < L::Q; ++c) f[c] += T(3) * wt<L, T>(c) * cdot<L, T>(c, gx, gy, gz) * (tem - tem0);
+}
+// AD::ExternalForceHeatExchange (advection.h:87-95)
+template <class L, class T> __device__ __forceinline__ void ad_heatex(T *g, T tem, T beta) {
+    const T coef = beta * (T(1) - tem) / (T(1) + beta);
+#pragma unroll
+    for (int c = 0; c < L::Q; ++c) g[c] += wt<L, T>(c) * coef;
+}
+// ANS::Macro (adjointnavierstokes.h:15-57)
+template <class L, class T> __device__ __forceinline__ void ans_macro(const T *f, const T *u, T &ip, T *iu, T *im) {
+    const T uu = vdot<L, T>(u, u);
+    const T w0 = wt<L, T>(0);
+    ip = f[0] * w0 * (T(1) - T(1.5) * uu);
+#pragma unroll
+    for (int b = 0; b < 3; ++b) { iu[b] = -f[0] * w0 * u[b]; im[b] = T(0); }
+#pragma unroll
+    for (int c = 1; c < L::Q; ++c) {
+        const T ciu = cdot<L, T>(c, u[0], u[1], u[2]);
+        const T fei = f[c] * wt<L, T>(c);
+        ip += fei * (T(1) + T(3) * ciu + T(4.5) * ciu * ciu - T(1.5) * uu);
+#pragma unroll
+        for (int b = 0; b < L::ND; ++b) {
+            const T cb = T(comp<L>(c, b));
+            iu[b] += fei * (cb + T(3) * ciu * cb - u[b]);
+        }
+#pragma unroll
+        for (int b = 0; b < L::ND; ++b) {
+            const int cb = comp<L>(c, b);
+            if (cb == 1) im[b] += fei; else if (cb == -1) im[b] -= fei;
+        }
+    }
+    if (L::ND == 2) { iu[2] = T(0); im[2] = T(0); }
+}
+// ANS::Equilibrium (adjointnavierstokes.h:59-73)
+template <class L, class T> __device__ __forceinline__ T ans_feq(int c, const T *u, T ip, const T *iu) {
+    const T s = L::ND == 2
+        ? iu[0] * (T(L::cx(c)) - u[0]) + iu[1] * (T(L::cy(c)) - u[1])
+        : iu[0] * (T(L::cx(c)) - u[0]) + iu[1] * (T(L::cy(c)) - u[1]) + iu[2] * (T(L::cz(c)) - u[2]);
+    return ip + T(3) * s;
+}
+// ANS::ExternalForceBrinkman (adjointnavierstokes.h:75-93)
+template <class L, class T> __device__ __forceinline__ void ans_brinkman(T *f, T rho, const T *u, const T *im, T alpha) {
+    const T coef = T(3) * alpha / (rho + alpha);
+    f[0] -= -coef * vdot<L, T>(u, im);
+#pragma unroll
+    for (int c = 1; c < L::Q; ++c) {
+        const T s = L::ND == 2
+            ? (T(L::cx(c)) - u[0]) * im[0] + (T(L::cy(c)) - u[1]) * im[1]
+            : (T(L::cx(c)) - u[0]) * im[0] + (T(L::cy(c)) - u[1]) * im[1] + (T(L::cz(c)) - u[2]) * im[2];
+        f[c] -= coef * s;
+    }
+}
+// AAD::Macro (adjointadvection.h:22-50)
+template <class L, class T> __device__ __forceinline__ void aad_macro(const T *g, T &item, T *iq) {
+    T it = wt<L, T>(0) * g[0], s0 = T(0), s1 = T(0), s2 = T(0);
+#pragma unroll
+    for (int c = 1; c < L::Q; ++c) {
+        const T gei = wt<L, T>(c) * g[c];
+        it += gei;
+        if (L::cx(c) == 1) s0 += gei; else if (L::cx(c) == -1) s0 -= gei;
+        if (L::cy(c) == 1) s1 += gei; else if (L::cy(c) == -1) s1 -= gei;
+        if (L::cz(c) == 1) s2 += gei; else if (L::cz(c) == -1) s2 -= gei;
+    }
+    item = it;
+    iq[0] = s0; iq[1] = s1; iq[2] = s2;
+}
+// AAD::ExternalForceBrinkman (adjointadvection.h:70-102)
+template <class L, class T> __device__ __forceinline__ void aad_brinkman(T *f, T rho, const T *u, const T *im, T tem,
+                                                                        const T *iq, T omg, T alpha) {
+    const T coef = T(3) / (rho + alpha);
+    T X[3];
+#pragma unroll
+    for (int b = 0; b < 3; ++b) X[b] = tem * iq[b] * omg - alpha * im[b];
+    const T s0 = L::ND == 2 ? -u[0] * X[0] + -u[1] * X[1] : -u[0] * X[0] + -u[1] * X[1] + -u[2] * X[2];
+    f[0] += coef * s0;
+#pragma unroll
+    for (int c = 1; c < L::Q; ++c) {
+        const T s = L::ND == 2
+            ? (T(L::cx(c)) - u[0]) * X[0] + (T(L::cy(c)) - u[1]) * X[1]
+            : (T(L::cx(c)) - u[0]) * X[0] + (T(L::cy(c)) - u[1]) * X[1] + (T(L::cz(c)) - u[2]) * X[2];
+        f[c] += coef * s;
+    }
+}
+// AAD::ExternalForceHeatExchange (adjointadvection.h:104-112)
+template <class L, class T> __device__ __forceinline__ void aad_heatex(T *g, T item, T beta) {
+    const T coef = beta * (T(1) + item) / (T(1) + beta);
+#pragma unroll
+    for (int c = 0; c < L::Q; ++c) g[c] -= coef;
+}
+// AAD::ExternalForceNaturalConvection (adjointadvection.h:114-132)
+template <class L, class T> __device__ __forceinline__ void aad_nc(T *g, const T *im, const T *gv) {
+    const T coef = T(3) * vdot<L, T>(im, gv);
+#pragma unroll
+    for (int c = 0; c < L::Q; ++c) g[c] += coef;
+}
+// AAD::ExternalForceMassFlow (adjointadvection.h:134-150)
+template <class L, class T> __device__ __forceinline__ void aad_massflow(T *f, T rho, const T *u, const T *dv) {
+    f[0] += vdot<L, T>(u, dv) / rho;
+#pragma unroll
+    for (int c = 1; c < L::Q; ++c) {
+        const T s = L::ND == 2
+            ? (T(L::cx(c)) - u[0]) * dv[0] + (T(L::cy(c)) - u[1]) * dv[1]
+            : (T(L::cx(c)) - u[0]) * dv[0] + (T(L::cy(c)) - u[1]) * dv[1] + (T(L::cz(c)) - u[2]) * dv[2];
+        f[c] -= s / rho;
+    }
+}
+
+template <class T> __device__ __forceinline__ T ldT(const void *p, int idx) { return static_cast<const T *>(p)[idx]; }
+
+// Macro + forces + BGK for one node, one reference collide routine per kind:
+// NS::MacroCollide / MacroBrinkmanCollide (navierstokes.h:430-546); AD::MacroCollide{Force,
+// Natural}Convection, MacroBrinkmanCollide{HeatExchange,ForceConvection,NaturalConvection}
+// (advection.h:528-1044); ANS::MacroBrinkmanCollide (adjointnavierstokes.h:396-470);
+// AAD::MacroBrinkmanCollide{HeatExchange,ForceConvection,NaturalConvection,
+// NaturalConvectionMassFlow} (adjointadvection.h:892-1355).
+// f, g: pre-collision populations in, post-collision out. When `snap` is non-null the
+// snapshot (the g populations at the point the reference saves them) is written to it.
+template <class L, class T, int K>
+__device__ __forceinline__ void collide_node(T *f, T *g, int idx, const KArgs &a, bool save, double *snap,
+                                             long long np, T *uout) {
+    constexpr int Q = L::Q;
+    const T omf = T(1) / (T(3) * T(a.ph.nu) + T(0.5));
+    T omg = T(0);
+    if (K == K_AD_NATURAL || K == K_AD_FORCE || K == K_AAD_NATURAL || K == K_AAD_FORCE || K == K_AAD_MASSFLOW)
+        omg = T(1) / (T(3) * ldT<T>(a.kappa, idx) + T(0.5));
+    else if (kind_has_g(K))
+        omg = T(1) / (T(3) * T(a.ph.diff) + T(0.5));
+    const T gv[3] = {T(a.ph.gx), T(a.ph.gy), T(a.ph.gz)};
+    if (K < 10) {
+        T rho, u[3], tem = T(0), q[3] = {T(0), T(0), T(0)};
+        ns_macro<L, T>(f, rho, u);
+        if (kind_has_g(K)) ad_macro<L, T>(g, u, omg, tem, q);
+        if (K == K_NS_BRINKMAN || K == K_AD_FORCE || K == K_AD_HEATEX) {
+            ns_brinkman<L, T>(f, rho, u, ldT<T>(a.alpha, idx));
+            ns_macro<L, T>(f, rho, u);
+            if (K == K_AD_HEATEX) ad_heatex<L, T>(g, tem, ldT<T>(a.beta, idx));
+            if (kind_has_g(K)) ad_macro<L, T>(g, u, omg, tem, q);
+        } else if (K == K_AD_NATURAL) {
+            ad_nc_force<L, T>(f, tem, gv[0], gv[1], gv[2], T(a.ph.tem0));
+            ns_brinkman<L, T>(f, rho, u, ldT<T>(a.alpha, idx));
+            ns_macro<L, T>(f, rho, u);
+            ad_macro<L, T>(g, u, omg, tem, q);
+        } else if (K == K_AD_NATURAL_NOBRINK) {
+            ad_nc_force<L, T>(f, tem, gv[0], gv[1], gv[2], T(a.ph.tem0));
+            ns_macro<L, T>(f, rho, u);
+            ad_macro<L, T>(g, u, omg, tem, q);
+        }
+        if (save) {
+            if (a.out[0]) a.out[0][idx] = double(rho);
+            if (a.out[1]) a.out[1][idx] = double(u[0]);
+            if (a.out[2]) a.out[2][idx] = double(u[1]);
+            if (L::ND == 3 && a.out[3]) a.out[3][idx] = double(u[2]);
+            if (kind_has_g(K)) {
+                if (a.out[4]) a.out[4][idx] = double(tem);
+                if (a.out[5]) a.out[5][idx] = double(q[0]);
+                if (a.out[6]) a.out[6][idx] = double(q[1]);
+                if (L::ND == 3 && a.out[7]) a.out[7][idx] = double(q[2]);
+            }
+        }
+        if (uout) { uout[0] = u[0]; uout[1] = u[1]; uout[2] = u[2]; }
+        if (snap && kind_has_snapshot(K)) {
+#pragma unroll
+            for (int c = 0; c < Q; ++c) snap[c * np + idx] = double(g[c]);
+        }
+        const T uu = ns_uu<L, T>(u);
+        const T iomf = T(1) - omf;
+#pragma unroll
+        for (int c = 0; c < Q; ++c) f[c] = iomf * f[c] + omf * ns_feq<L, T>(c, rho, u, uu);
+        if (kind_has_g(K)) {
+            const T iomg = T(1) - omg;
+#pragma unroll
+            for (int c = 0; c < Q; ++c) g[c] = iomg * g[c] + omg * ad_geq<L, T>(c, tem, u);
+        }
+    } else {
+        const T rho = ldT<T>(a.fwd[0], idx);
+        const T u[3] = {ldT<T>(a.fwd[1], idx), ldT<T>(a.fwd[2], idx), L::ND == 3 ? ldT<T>(a.fwd[3], idx) : T(0)};
+        T ip, iu[3], im[3], item = T(0), iq[3] = {T(0), T(0), T(0)};
+        ans_macro<L, T>(f, u, ip, iu, im);
+        if (K == K_ANS_BRINKMAN) {
+            ans_brinkman<L, T>(f, rho, u, im, ldT<T>(a.alpha, idx));
+            ans_macro<L, T>(f, u, ip, iu, im);
+        } else {
+            const T tem = ldT<T>(a.fwd[4], idx);
+            aad_macro<L, T>(g, item, iq);
+            if (K == K_AAD_MASSFLOW) {
+                const T dv[3] = {ldT<T>(a.dirx, idx), ldT<T>(a.diry, idx), L::ND == 3 ? ldT<T>(a.dirz, idx) : T(0)};
+                aad_massflow<L, T>(f, rho, u, dv);
+            }
+            aad_brinkman<L, T>(f, rho, u, im, tem, iq, omg, ldT<T>(a.alpha, idx));
+            ans_macro<L, T>(f, u, ip, iu, im);
+            if (K == K_AAD_NATURAL || K == K_AAD_MASSFLOW) {
+                aad_nc<L, T>(g, im, gv);
+                aad_macro<L, T>(g, item, iq);
+            } else if (K == K_AAD_HEATEX) {
+                aad_heatex<L, T>(g, item, ldT<T>(a.beta, idx));
+                aad_macro<L, T>(g, item, iq);
+            }
+        }
+        if (save) {
+            if (a.out[0]) a.out[0][idx] = double(ip);
+            if (a.out[1]) a.out[1][idx] = double(iu[0]);
+            if (a.out[2]) a.out[2][idx] = double(iu[1]);
+            // the D3Q15 ForceConvection adjoint never stores iuz (adjointadvection.h:1074-1084)
+            if (L::ND == 3 && K != K_AAD_FORCE && a.out[3]) a.out[3][idx] = double(iu[2]);
+            if (a.out[4]) a.out[4][idx] = double(im[0]);
+            if (a.out[5]) a.out[5][idx] = double(im[1]);
+            if (L::ND == 3 && a.out[6]) a.out[6][idx] = double(im[2]);
+            if (kind_has_g(K)) {
+                if (a.out[7]) a.out[7][idx] = double(item);
+                if (a.out[8]) a.out[8][idx] = double(iq[0]);
+                if (a.out[9]) a.out[9][idx] = double(iq[1]);
+                if (L::ND == 3 && a.out[10]) a.out[10][idx] = double(iq[2]);
+            }
+        }
+        if (snap && kind_has_snapshot(K)) {
+#pragma unroll
+            for (int c = 0; c < Q; ++c) snap[c * np + idx] = double(g[c]);
+        }
+        const T iomf = T(1) - omf;
+#pragma unroll
+        for (int c = 0; c < Q; ++c) f[c] = iomf * f[c] + omf * ans_feq<L, T>(c, u, ip, iu);
+        if (kind_has_g(K)) {
+            const T geq = item + T(3) * vdot<L, T>(u, iq);
+            const T iomg = T(1) - omg;
+#pragma unroll
+            for (int c = 0; c < Q; ++c) g[c] = iomg * g[c] + omg * geq;
+        }
+    }
+}
+
+}  // namespace pl
