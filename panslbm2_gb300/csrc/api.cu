@@ -46,6 +46,18 @@ struct Program {
     Op *ops = nullptr;
     uint8_t *flags = nullptr;
     uint32_t face_mask = 0;
+    // staged boundary path
+    bool staged = false;
+    int ndir = 0, ndir_all = 0, ns = 0, nt = 0;
+    int *icode = nullptr;
+    pl::InlineRec *irec = nullptr;
+    int *dnode = nullptr, *dstart = nullptr, *snode = nullptr, *sstart = nullptr, *tslot = nullptr;
+    int *dnode_all = nullptr, *dstart_all = nullptr;
+    Op *dops = nullptr, *sops = nullptr, *dops_all = nullptr;
+    pl::SmoothEntry *sent = nullptr;
+    std::vector<int> gstart;
+    int *d_gstart = nullptr;
+    void *tbuf = nullptr;
 };
 
 struct Taps {
@@ -91,6 +103,8 @@ struct pl_lattice_s {
     int *iscratch = nullptr;
     std::map<std::pair<int, long long>, Taps> taps;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaStream_t side = nullptr, side2 = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_join2 = nullptr;
     double last_ms = 0.0;
     long long launches = 0;
     LaunchFn launch = nullptr;
@@ -279,7 +293,14 @@ int compile_program(pl_lattice h, const pl_bc_desc *descs, int ndesc, Program &P
         }
     }
     bstart.push_back((int)ops.size());
-    // skip mode: geometric when every op node lies on a domain face
+    // every node whose state a smoothing op reads belongs to the boundary set as well
+    std::vector<int> req = opnodes;
+    for (const Op &o : ops)
+        if (o.kind == pl::BC_SMOOTH)
+            for (int m = 0; m < o.sub; ++m) req.push_back(o.nbr[m]);
+    std::sort(req.begin(), req.end());
+    req.erase(std::unique(req.begin(), req.end()), req.end());
+    // skip mode: geometric when every such node lies on a domain face
     auto on_face_bits = [&](int idx) {
         const int i = idx % h->nx, r = idx / h->nx, j = r % h->ny, k = r / h->ny;
         uint32_t m = 0;
@@ -289,7 +310,7 @@ int compile_program(pl_lattice h, const pl_bc_desc *descs, int ndesc, Program &P
     };
     bool geometric = true;
     uint32_t mask = 0;
-    for (int nd_ : opnodes) {
+    for (int nd_ : req) {
         const uint32_t m = on_face_bits(nd_);
         if (!m) { geometric = false; break; }
         mask |= m;
@@ -299,14 +320,118 @@ int compile_program(pl_lattice h, const pl_bc_desc *descs, int ndesc, Program &P
     if (geometric) {
         for (int idx = 0; idx < h->n; ++idx) if (on_face_bits(idx) & mask) bnodes.push_back(idx);
     } else {
-        bnodes = opnodes;
+        bnodes = req;
         flags.assign(h->n, 0);
-        for (int nd_ : opnodes) flags[nd_] = 1;
+        for (int nd_ : req) flags[nd_] = 1;
     }
     P.nb = (int)bnodes.size();
     P.nops = (int)ops.size();
     P.nslot = (int)opnodes.size();
     P.face_mask = geometric ? mask : 0;
+
+    // staged path: valid when, at every node, the non-smoothing ops all come before the
+    // smoothing ops, and every node a smoothing op reads has no non-smoothing op after it
+    std::vector<int> bslot(h->n, -1);
+    for (int b = 0; b < P.nb; ++b) bslot[bnodes[b]] = b;
+    std::vector<int> last_plain(h->n, -1), first_smooth(h->n, 0x7fffffff);
+    for (const Op &o : ops) {
+        if (o.kind == pl::BC_SMOOTH) first_smooth[o.node] = std::min(first_smooth[o.node], o.seq);
+        else last_plain[o.node] = std::max(last_plain[o.node], o.seq);
+    }
+    bool staged = true;
+    for (const Op &o : ops) {
+        if (o.kind != pl::BC_SMOOTH) continue;
+        if (last_plain[o.node] > first_smooth[o.node]) staged = false;
+        for (int m = 0; m < o.sub; ++m) if (last_plain[o.nbr[m]] > o.seq) staged = false;
+    }
+    // direct set D (boundary nodes no smoothing op writes), staged set S (nodes smoothing reads
+    // or writes), targets T (nodes smoothing writes)
+    std::vector<int> dnode, dstart, snode, sstart, tslot, dnode_all, dstart_all, icode;
+    std::vector<pl::InlineRec> irec;
+    std::vector<Op> dops, sops, dops_all;
+    std::vector<pl::SmoothEntry> sent;
+    if (staged) {
+        std::vector<char> is_t(h->n, 0), is_s(h->n, 0);
+        for (const Op &o : ops)
+            if (o.kind == pl::BC_SMOOTH) {
+                is_t[o.node] = is_s[o.node] = 1;
+                for (int m = 0; m < o.sub; ++m) is_s[o.nbr[m]] = 1;
+            }
+        auto plain_ops = [&](int node, std::vector<Op> &out) {
+            const int sl = slot_of[node];
+            if (sl >= 0)
+                for (int o = bstart[sl]; o < bstart[sl + 1]; ++o)
+                    if (ops[o].kind != pl::BC_SMOOTH) out.push_back(ops[o]);
+        };
+        // interior codes: smoothing targets and nodes with ops the interior kernel does not
+        // apply go to the side path; other op nodes are applied inline (inline kinds) or by
+        // the direct kernel (other kinds)
+        icode.assign(h->n, -1);
+        for (size_t sl = 0; sl < opnodes.size(); ++sl) {
+            const int node = opnodes[sl];
+            if (is_t[node]) { icode[node] = -2; continue; }
+            bool simple = bstart[sl + 1] - bstart[sl] <= pl::kInlineMaxOps;
+            for (int o = bstart[sl]; o < bstart[sl + 1]; ++o)
+                if (!pl::op_is_simple(ops[o].kind)) simple = false;
+            if (simple) {
+                pl::InlineRec rec;
+                memset(&rec, 0, sizeof rec);
+                for (int o = bstart[sl]; o < bstart[sl + 1]; ++o) {
+                    const Op &op = ops[o];
+                    const int m = o - bstart[sl];
+                    const uint32_t b = (uint32_t)pl::simple_index(op.kind) | ((uint32_t)op.axis << 3) |
+                                       (op.dir > 0 ? 32u : 0u) | (op.lat ? 64u : 0u) | (op.sub == 2 ? 128u : 0u);
+                    rec.code |= b << (8 * m);
+                    rec.v[m] = (op.kind == pl::BC_AAD_Q) ? op.eps : op.v0;
+                    rec.w[m] = op.v1;
+                }
+                rec.nops = (uint32_t)(bstart[sl + 1] - bstart[sl]);
+                icode[node] = (int)irec.size();
+                irec.push_back(rec);
+            } else {
+                icode[node] = -2;
+            }
+            if (!simple) { dnode.push_back(node); dstart.push_back((int)dops.size()); plain_ops(node, dops); }
+            dnode_all.push_back(node); dstart_all.push_back((int)dops_all.size()); plain_ops(node, dops_all);
+        }
+        dstart.push_back((int)dops.size());
+        dstart_all.push_back((int)dops_all.size());
+        if (!geometric)
+            for (int node = 0; node < h->n; ++node) if (is_s[node]) flags[node] = 1;
+        std::vector<int> sslot(h->n, -1);
+        for (int node = 0; node < h->n; ++node)
+            if (is_s[node]) { sslot[node] = (int)snode.size(); snode.push_back(node); sstart.push_back((int)sops.size()); plain_ops(node, sops); }
+        sstart.push_back((int)sops.size());
+        for (int node = 0; node < h->n; ++node) if (is_t[node]) tslot.push_back(sslot[node]);
+        // smoothing ops in call order, scheduled into dependency levels (per population set:
+        // read-after-write, write-after-read and write-after-write order is kept)
+        std::vector<const Op *> sm;
+        for (const Op &o : ops) if (o.kind == pl::BC_SMOOTH) sm.push_back(&o);
+        std::stable_sort(sm.begin(), sm.end(), [](const Op *x, const Op *y) { return x->seq < y->seq; });
+        const size_t NS = snode.size();
+        std::vector<int> lw(2 * NS, 0), lr(2 * NS, 0);
+        std::vector<std::vector<pl::SmoothEntry>> lev;
+        for (const Op *o : sm) {
+            const size_t L0 = o->lat ? NS : 0;
+            const int self = sslot[o->node];
+            int lvl = std::max(lw[L0 + self], lr[L0 + self]);
+            for (int m = 0; m < o->sub; ++m) lvl = std::max(lvl, lw[L0 + sslot[o->nbr[m]]]);
+            lvl += 1;
+            lw[L0 + self] = lvl;
+            for (int m = 0; m < o->sub; ++m) lr[L0 + sslot[o->nbr[m]]] = std::max(lr[L0 + sslot[o->nbr[m]]], lvl);
+            if ((int)lev.size() < lvl) lev.resize(lvl);
+            pl::SmoothEntry e;
+            memset(&e, 0, sizeof e);
+            e.slot = self; e.lat = o->lat; e.nnbr = (int8_t)o->sub;
+            for (int m = 0; m < 3; ++m) e.nbr[m] = m < o->sub ? sslot[o->nbr[m]] : 0;
+            lev[lvl - 1].push_back(e);
+        }
+        P.gstart.assign(1, 0);
+        for (auto &l : lev) { sent.insert(sent.end(), l.begin(), l.end()); P.gstart.push_back((int)sent.size()); }
+        P.ndir = (int)dnode.size(); P.ndir_all = (int)dnode_all.size(); P.ns = (int)snode.size(); P.nt = (int)tslot.size();
+    }
+    P.staged = staged;
+
     int r;
     if ((r = dalloc((void **)&P.slot_of, sizeof(int) * h->n))) return r;
     CK(cudaMemcpyAsync(P.slot_of, slot_of.data(), sizeof(int) * h->n, cudaMemcpyHostToDevice, h->st));
@@ -320,6 +445,37 @@ int compile_program(pl_lattice h, const pl_bc_desc *descs, int ndesc, Program &P
         if ((r = dalloc((void **)&P.ops, sizeof(Op) * P.nops))) return r;
         CK(cudaMemcpyAsync(P.ops, ops.data(), sizeof(Op) * P.nops, cudaMemcpyHostToDevice, h->st));
     }
+    if (staged && P.nb) {
+        auto up_i = [&](int **dst, const std::vector<int> &v) -> int {
+            if (v.empty()) return PL_OK;
+            int rr = dalloc((void **)dst, sizeof(int) * v.size());
+            if (rr) return rr;
+            CK(cudaMemcpyAsync(*dst, v.data(), sizeof(int) * v.size(), cudaMemcpyHostToDevice, h->st));
+            return PL_OK;
+        };
+        auto up_o = [&](Op **dst, const std::vector<Op> &v) -> int {
+            if (v.empty()) return PL_OK;
+            int rr = dalloc((void **)dst, sizeof(Op) * v.size());
+            if (rr) return rr;
+            CK(cudaMemcpyAsync(*dst, v.data(), sizeof(Op) * v.size(), cudaMemcpyHostToDevice, h->st));
+            return PL_OK;
+        };
+        if ((r = up_i(&P.dnode, dnode)) || (r = up_i(&P.dstart, dstart)) || (r = up_i(&P.snode, snode)) ||
+            (r = up_i(&P.sstart, sstart)) || (r = up_i(&P.tslot, tslot)) || (r = up_o(&P.dops, dops)) ||
+            (r = up_o(&P.sops, sops)) || (r = up_i(&P.dnode_all, dnode_all)) ||
+            (r = up_i(&P.dstart_all, dstart_all)) || (r = up_o(&P.dops_all, dops_all)) || (r = up_i(&P.icode, icode)))
+            return r;
+        if (!irec.empty()) {
+            if ((r = dalloc((void **)&P.irec, sizeof(pl::InlineRec) * irec.size()))) return r;
+            CK(cudaMemcpyAsync(P.irec, irec.data(), sizeof(pl::InlineRec) * irec.size(), cudaMemcpyHostToDevice, h->st));
+        }
+        if (!sent.empty()) {
+            if ((r = dalloc((void **)&P.sent, sizeof(pl::SmoothEntry) * sent.size()))) return r;
+            CK(cudaMemcpyAsync(P.sent, sent.data(), sizeof(pl::SmoothEntry) * sent.size(), cudaMemcpyHostToDevice, h->st));
+        }
+        if (P.ns && (r = dalloc(&P.tbuf, h->csize * 2 * h->q * (size_t)P.ns))) return r;
+        if ((r = up_i(&P.d_gstart, P.gstart))) return r;
+    }
     if (!geometric) {
         if ((r = dalloc((void **)&P.flags, h->n))) return r;
         CK(cudaMemcpyAsync(P.flags, flags.data(), h->n, cudaMemcpyHostToDevice, h->st));
@@ -331,6 +487,9 @@ int compile_program(pl_lattice h, const pl_bc_desc *descs, int ndesc, Program &P
 
 void free_program(Program &P) {
     cudaFree(P.bnode); cudaFree(P.bstart); cudaFree(P.slot_of); cudaFree(P.ops); cudaFree(P.flags);
+    cudaFree(P.dnode); cudaFree(P.dstart); cudaFree(P.snode); cudaFree(P.sstart); cudaFree(P.tslot);
+    cudaFree(P.dops); cudaFree(P.sops); cudaFree(P.sent); cudaFree(P.tbuf); cudaFree(P.d_gstart);
+    cudaFree(P.icode); cudaFree(P.irec); cudaFree(P.dnode_all); cudaFree(P.dstart_all); cudaFree(P.dops_all);
     P = Program();
 }
 
@@ -349,6 +508,7 @@ int build_args(pl_lattice h, int kind, const pl_phys *ph, int prog, int src, int
     a.save = save ? 1 : 0;
     a.err = h->err;
     const bool adjk = pl::kind_is_adjoint(kind);
+    a.sgn = adjk ? 1 : -1;
     // inputs required by the kind
     int r;
     if (!kind_inputs) goto program;
@@ -399,6 +559,17 @@ program:
         const Program &P = h->progs[prog];
         a.bnode = P.bnode; a.bstart = P.bstart; a.ops = P.ops; a.slot_of = P.slot_of; a.nb = P.nb;
         a.geo.face_mask = P.face_mask; a.geo.flags = P.flags;
+        a.staged = P.staged ? 1 : 0;
+        a.ns = P.ns; a.nt = P.nt;
+        a.icode = P.staged ? P.icode : nullptr;
+        a.irec = P.irec;
+        if (pl::kind_inline_bc(kind) && kind_inputs) { a.ndir = P.ndir; a.dnode = P.dnode; a.dstart = P.dstart; a.dops = P.dops; }
+        else { a.ndir = P.ndir_all; a.dnode = P.dnode_all; a.dstart = P.dstart_all; a.dops = P.dops_all; }
+        a.snode = P.snode; a.sstart = P.sstart; a.sops = P.sops; a.tslot = P.tslot;
+        a.sent = P.sent; a.tbuf = P.tbuf;
+        a.h_gstart = P.gstart.data(); a.gstart = P.d_gstart;
+        a.ngroups = P.gstart.empty() ? 0 : (int)P.gstart.size() - 1;
+        a.side = h->side; a.side2 = h->side2; a.ev_fork = h->ev_fork; a.ev_join = h->ev_join; a.ev_join2 = h->ev_join2;
         // velocity read by AD/AAD ops
         if (!adjk) {
             const int s = bcu_slot >= 0 ? bcu_slot : 0;
@@ -461,7 +632,7 @@ int do_step(pl_lattice h, int kind, const pl_phys *ph, int prog, bool save) {
     int r = build_args(h, kind, ph, prog, h->cur, h->cur ^ 1, save, true, bcu_slot, a);
     if (r) return r;
     if (h->launch(kind, pl::OP_STEP, save, a, h->st)) return fail(PL_ERR_UNSUPPORTED, "kind %d not built for this storage", kind);
-    if ((r = check_launch(h, a.nb > 0 ? 2 : 1))) return r;
+    if ((r = check_launch(h, a.nb > 0 ? (a.staged ? 1 + (a.ndir > 0) + (a.ns > 0 ? 2 + a.ngroups : 0) : 2) : 1))) return r;
     after_collide(h, kind, save, h->cur, prog, true, bcu_slot, ph);
     h->cur ^= 1;
     return PL_OK;
@@ -586,6 +757,15 @@ int pl_create(int q, int nx, int ny, int nz, int storage, pl_lattice *out) {
     cudaMemsetAsync(h->err, 0, sizeof(int), h->st);
     cudaEventCreate(&h->ev0);
     cudaEventCreate(&h->ev1);
+    // boundary chains run on high-priority streams so their blocks are scheduled as soon as the
+    // interior kernel frees resources, instead of after its last block has been dispatched
+    int prio_lo = 0, prio_hi = 0;
+    cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
+    cudaStreamCreateWithPriority(&h->side, cudaStreamNonBlocking, prio_hi);
+    cudaStreamCreateWithPriority(&h->side2, cudaStreamNonBlocking, prio_hi);
+    cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&h->ev_join2, cudaEventDisableTiming);
     if (cudaStreamSynchronize(h->st) != cudaSuccess) { pl_destroy(h); return fail(PL_ERR_CUDA, "init failed"); }
     *out = h;
     return PL_OK;
@@ -604,6 +784,11 @@ int pl_destroy(pl_lattice h) {
     cudaFree(h->iscratch); cudaFree(h->partial); cudaFree(h->nonfinite); cudaFree(h->err); cudaFree(h->dout);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
+    if (h->side) { cudaStreamSynchronize(h->side); cudaStreamDestroy(h->side); }
+    if (h->side2) { cudaStreamSynchronize(h->side2); cudaStreamDestroy(h->side2); }
+    if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+    if (h->ev_join) cudaEventDestroy(h->ev_join);
+    if (h->ev_join2) cudaEventDestroy(h->ev_join2);
     if (h->own_stream && h->st) cudaStreamDestroy(h->st);
     delete h;
     return PL_OK;

@@ -67,28 +67,39 @@ __device__ __forceinline__ void tang3(int a, int &t0, int &t1) {
     t1 = a == 0 ? 2 : (a == 1 ? 0 : 1);
 }
 
+// wall copy on one population set; every array index is a compile-time constant after
+// unrolling (the runtime axis only selects among constants), so the set stays in registers
 template <class L, class T>
-__device__ __noinline__ void apply_op(const Op &op, T *f, T *g, int node, const KArgs &a) {
+__device__ __forceinline__ void wall_set(T *p, int A, int d, bool adj, int type) {
+    constexpr int Q = L::Q;
+    T src[Q];
+#pragma unroll
+    for (int c = 0; c < Q; ++c) src[c] = p[c];
+#pragma unroll
+    for (int c = 1; c < Q; ++c) {
+        const int ca = A == 0 ? L::cx(c) : (A == 1 ? L::cy(c) : L::cz(c));
+        if (adj ? (ca != d) : (ca != -d)) continue;
+        const T r = A == 0 ? src[refl<L>(c, 0)] : (A == 1 ? src[refl<L>(c, 1)] : src[refl<L>(c, 2)]);
+        p[c] = type == 1 ? src[opp<L>(c)] : r;
+    }
+}
+
+template <class L, class T, bool SIMPLE = false>
+__device__ __forceinline__ void apply_op(const Op &op, T *f, T *g, int node, const KArgs &a,
+                                         const T *upre = nullptr, T kpre = T(0)) {
     const int A = op.axis, d = op.dir, nin = -d;
     constexpr int Q = L::Q, ND = L::ND;
+    if (SIMPLE && !op_is_simple(op.kind)) return;
     switch (op.kind) {
     case BC_WALL:
     case BC_IWALL: {
-        T *p = op.lat ? g : f;
         const bool adj = op.kind == BC_IWALL;
-        T src[Q];
-#pragma unroll
-        for (int c = 0; c < Q; ++c) src[c] = p[c];
-#pragma unroll
-        for (int c = 1; c < Q; ++c) {
-            const int ca = cmp<L>(c, A);
-            if (adj ? (ca != d) : (ca != -d)) continue;
-            p[c] = op.sub == 1 ? src[opp_d<L>(c)] : src[refl_d<L>(c, A)];
-        }
+        if (op.lat) wall_set<L, T>(g, A, d, adj, op.sub);
+        else wall_set<L, T>(f, A, d, adj, op.sub);
         break;
     }
     case BC_NS_U:
-    case BC_NS_RHO: {
+    case BC_NS_RHO: if constexpr (!SIMPLE) {
         T *p = f;
         T u[3] = {T(0), T(0), T(0)};
         T sT = T(0), sO = T(0);
@@ -147,12 +158,14 @@ __device__ __noinline__ void apply_op(const Op &op, T *f, T *g, int node, const 
             p[c] = v;
         }
         break;
-    }
+    } break;
     case BC_AD_T:
     case BC_AD_Q:
     case BC_AD_QC: {
         T *p = g;
-        const T u[3] = {T(a.bcu[0][node]), T(a.bcu[1][node]), ND == 3 ? T(a.bcu[2][node]) : T(0)};
+        T u[3];
+        if (upre) { u[0] = upre[0]; u[1] = upre[1]; u[2] = upre[2]; }
+        else { u[0] = T(a.bcu[0][node]); u[1] = T(a.bcu[1][node]); u[2] = ND == 3 ? T(a.bcu[2][node]) : T(0); }
         T tem0;
         if (op.kind == BC_AD_T) {
             T s = T(op.v0);
@@ -160,7 +173,7 @@ __device__ __noinline__ void apply_op(const Op &op, T *f, T *g, int node, const 
             for (int c = 0; c < Q; ++c) if (cmp<L>(c, A) != -d) s -= p[c];
             tem0 = T(6) * s / (nin > 0 ? T(1) + T(3) * u[A] : T(1) - T(3) * u[A]);
         } else {
-            const T kap = op.kind == BC_AD_Q ? T(a.bckappa[node]) : T(op.v1);
+            const T kap = op.kind == BC_AD_Q ? (upre ? kpre : T(a.bckappa[node])) : T(op.v1);
             T s = (T(1) + T(1) / (T(6) * kap)) * T(op.v0);
 #pragma unroll
             for (int c = 1; c < Q; ++c) if (cmp<L>(c, A) == d) s += p[c];
@@ -172,7 +185,7 @@ __device__ __noinline__ void apply_op(const Op &op, T *f, T *g, int node, const 
         break;
     }
     case BC_ANS_U:
-    case BC_ANS_RHO: {
+    case BC_ANS_RHO: if constexpr (!SIMPLE) {
         T *p = f;
         T rho0;
         if (op.kind == BC_ANS_RHO) {
@@ -212,11 +225,13 @@ __device__ __noinline__ void apply_op(const Op &op, T *f, T *g, int node, const 
 #pragma unroll
         for (int c = 1; c < Q; ++c) if (cmp<L>(c, A) == d) p[c] = src[opp_d<L>(c)] + rho0;
         break;
-    }
+    } break;
     case BC_AAD_T:
     case BC_AAD_Q: {
         T *p = g;
-        const T u[3] = {T(a.bcu[0][node]), T(a.bcu[1][node]), ND == 3 ? T(a.bcu[2][node]) : T(0)};
+        T u[3];
+        if (upre) { u[0] = upre[0]; u[1] = upre[1]; u[2] = upre[2]; }
+        else { u[0] = T(a.bcu[0][node]); u[1] = T(a.bcu[1][node]); u[2] = ND == 3 ? T(a.bcu[2][node]) : T(0); }
         const T pre = nin > 0 ? T(1) + T(3) * u[A] : T(1) - T(3) * u[A];
         const T post = nin > 0 ? T(1) - T(3) * u[A] : T(1) + T(3) * u[A];
         T rho0;
@@ -261,7 +276,7 @@ __device__ __noinline__ void apply_op(const Op &op, T *f, T *g, int node, const 
         for (int c = 1; c < Q; ++c) if (cmp<L>(c, A) == d) p[c] = rho0;
         break;
     }
-    case BC_AAD_RHO: {
+    case BC_AAD_RHO: if constexpr (!SIMPLE) {
         const T u[3] = {T(a.bcu[0][node]), T(a.bcu[1][node]), ND == 3 ? T(a.bcu[2][node]) : T(0)};
         const T rho = T(a.bcrho[node]), tem = T(a.bctem[node]);
         const T pre = nin > 0 ? T(1) + T(3) * u[A] : T(1) - T(3) * u[A];
@@ -291,10 +306,16 @@ __device__ __noinline__ void apply_op(const Op &op, T *f, T *g, int node, const 
 #pragma unroll
         for (int c = 1; c < Q; ++c) if (cmp<L>(c, A) == d) f[c] = src[opp_d<L>(c)] + r0 + flux0 + obj0;
         break;
-    }
+    } break;
     default:
         break;
     }
+}
+
+// out-of-line copy for the recursive replay path (keeps code size bounded)
+template <class L, class T>
+__device__ __noinline__ void apply_op_ni(const Op &op, T *f, T *g, int node, const KArgs &a) {
+    apply_op<L, T>(op, f, g, node, a);
 }
 
 }  // namespace pl

@@ -15,6 +15,10 @@ __host__ __device__ constexpr bool kind_has_g(int k) { return !(k == K_NS_COLLID
 __host__ __device__ constexpr bool kind_node_kappa(int k) {
     return k == K_AD_NATURAL || k == K_AD_FORCE || k == K_AAD_NATURAL || k == K_AAD_FORCE || k == K_AAD_MASSFLOW;
 }
+// kinds whose interior kernel applies the simple boundary ops inline
+__host__ __device__ constexpr bool kind_inline_bc(int k) {
+    return k == K_AD_NATURAL || k == K_AD_FORCE || k == K_AAD_NATURAL || k == K_AAD_FORCE;
+}
 __host__ __device__ constexpr bool kind_has_snapshot(int k) {
     return k == K_AD_NATURAL || k == K_AD_FORCE || k == K_AAD_NATURAL || k == K_AAD_FORCE || k == K_AAD_MASSFLOW;
 }
@@ -24,6 +28,31 @@ enum BcKind {
     BC_WALL = 0, BC_IWALL = 1, BC_NS_U = 2, BC_NS_RHO = 3, BC_AD_T = 4, BC_AD_Q = 5, BC_AD_QC = 6,
     BC_ANS_U = 7, BC_ANS_RHO = 8, BC_AAD_T = 9, BC_AAD_Q = 10, BC_AAD_RHO = 11, BC_SMOOTH = 20
 };
+
+// ops the interior kernel applies inline (walls, AD SetT / SetQ, AAD iSetT / iSetQ)
+__host__ __device__ constexpr bool op_is_simple(int k) {
+    return k == BC_WALL || k == BC_IWALL || k == BC_AD_T || k == BC_AD_Q || k == BC_AD_QC || k == BC_AAD_T ||
+           k == BC_AAD_Q;
+}
+
+// Compact record of the simple ops of one boundary node, read by the interior kernel in one
+// round trip: op m is byte m of `code` (bits 0-2 simple kind index, 3-4 axis, 5 side (+1 when
+// set), 6 set (g when set), 7 wall type (MIRROR when set)); v[m] its value (T / qn / eps) and
+// w[m] its second value (constant kappa).
+struct InlineRec {
+    uint32_t code, nops;
+    double v[4], w[4];
+    uint64_t pad;
+};
+constexpr int kInlineMaxOps = 4;
+__host__ __device__ constexpr int simple_kind(int idx) {
+    return idx == 0 ? BC_WALL : idx == 1 ? BC_IWALL : idx == 2 ? BC_AD_T : idx == 3 ? BC_AD_Q : idx == 4 ? BC_AD_QC
+         : idx == 5 ? BC_AAD_T : BC_AAD_Q;
+}
+__host__ __device__ constexpr int simple_index(int k) {
+    return k == BC_WALL ? 0 : k == BC_IWALL ? 1 : k == BC_AD_T ? 2 : k == BC_AD_Q ? 3 : k == BC_AD_QC ? 4
+         : k == BC_AAD_T ? 5 : 6;
+}
 
 // One boundary-program op as applied at one node. `lat` selects the population set the op
 // writes (0 = NS set f, 1 = AD set g). For BC_SMOOTH, nnbr neighbours are averaged.
@@ -35,6 +64,13 @@ struct Op {
                                   // D3Q15 +x MIRROR quirk)
     int32_t nbr[3];
     double v0, v1, v2, eps;
+};
+
+// One smoothing update of the staged boundary path: node `slot` of set `lat` becomes the mean
+// of nnbr neighbour slots (all indices into the boundary scratch buffer).
+struct SmoothEntry {
+    int32_t slot, nbr[3];
+    int8_t lat, nnbr, pad[2];
 };
 
 struct Geo {
@@ -67,6 +103,26 @@ struct KArgs {
     const double *bcrho, *bctem;  // forward rho / T read by AAD iSetRho
     const double *bckappa;      // per-node kappa read by AD SetQ
     double *bcu_out[3];         // where this step stores the new velocity of boundary nodes
+    // staged boundary path. Boundary nodes no smoothing op writes take the direct kernel
+    // (dnode, CSR dstart/dops); the nodes smoothing reads or writes (snode, CSR sstart/sops)
+    // go through the scratch buffer: pre (ops) -> smoothing levels -> post (the nt targets).
+    int staged;
+    const int *icode;           // per node, read for face / flagged nodes: -1 no ops, -2 side
+                                // path, >= 0 index of its InlineRec (ops applied inline)
+    const InlineRec *irec;
+    int ndir, ns, nt;
+    const int *dnode, *dstart;
+    const Op *dops;
+    const int *snode, *sstart, *tslot;
+    const Op *sops;
+    const SmoothEntry *sent;    // smoothing entries, grouped by level (slots index snode)
+    const int *gstart;          // entry offsets of the levels (ngroups+1), device
+    const int *h_gstart;        // the same offsets, host
+    int ngroups;
+    void *tbuf;                 // scratch: 2*Q planes of ns compute-type values
+    void *side, *side2;         // host: cudaStream_t of the two boundary chains
+    void *ev_fork, *ev_join, *ev_join2;   // host: cudaEvent_t
+    int sgn;                    // -1 Stream, +1 iStream
     Phys ph;
     int pull;                   // 1: stream (pull) before the boundary program
     int save;                   // 1: write macro outputs

@@ -9,18 +9,116 @@ namespace pl {
 #define PL_CAT2(a, b) a##b
 #define PL_CAT(a, b) PL_CAT2(a, b)
 
+using TC = Store<PL_STORE>::T;
+
+// collide of a runtime kind (uniform over the grid), for the boundary kernels
+static __device__ __forceinline__ void collide_any(int kind, TC *f, TC *g, int idx, const KArgs &a, bool save, TC *u) {
+    switch (kind) {
+    case K_AD_NATURAL: collide_node<PL_LAT, TC, K_AD_NATURAL>(f, g, idx, a, save, nullptr, a.geo.np, u); break;
+    case K_AD_FORCE: collide_node<PL_LAT, TC, K_AD_FORCE>(f, g, idx, a, save, nullptr, a.geo.np, u); break;
+    case K_AAD_NATURAL: collide_node<PL_LAT, TC, K_AAD_NATURAL>(f, g, idx, a, save, nullptr, a.geo.np, nullptr); break;
+    case K_AAD_FORCE: collide_node<PL_LAT, TC, K_AAD_FORCE>(f, g, idx, a, save, nullptr, a.geo.np, nullptr); break;
+    case K_NS_COLLIDE: collide_node<PL_LAT, TC, K_NS_COLLIDE>(f, g, idx, a, save, nullptr, a.geo.np, u); break;
+#ifdef PL_ALL_KINDS
+    case K_NS_BRINKMAN: collide_node<PL_LAT, TC, K_NS_BRINKMAN>(f, g, idx, a, save, nullptr, a.geo.np, u); break;
+    case K_AD_HEATEX: collide_node<PL_LAT, TC, K_AD_HEATEX>(f, g, idx, a, save, nullptr, a.geo.np, u); break;
+    case K_AD_NATURAL_NOBRINK: collide_node<PL_LAT, TC, K_AD_NATURAL_NOBRINK>(f, g, idx, a, save, nullptr, a.geo.np, u); break;
+    case K_AD_FORCE_NOBRINK: collide_node<PL_LAT, TC, K_AD_FORCE_NOBRINK>(f, g, idx, a, save, nullptr, a.geo.np, u); break;
+    case K_ANS_BRINKMAN: collide_node<PL_LAT, TC, K_ANS_BRINKMAN>(f, g, idx, a, save, nullptr, a.geo.np, nullptr); break;
+    case K_AAD_HEATEX: collide_node<PL_LAT, TC, K_AAD_HEATEX>(f, g, idx, a, save, nullptr, a.geo.np, nullptr); break;
+    case K_AAD_MASSFLOW: collide_node<PL_LAT, TC, K_AAD_MASSFLOW>(f, g, idx, a, save, nullptr, a.geo.np, nullptr); break;
+#endif
+    default: break;
+    }
+}
+
+static __device__ __forceinline__ void finish_boundary(int kind, TC *f, TC *g, int node, const KArgs &a) {
+    constexpr int Q = PL_LAT::Q;
+    TC u[3] = {TC(0), TC(0), TC(0)};
+    collide_any(kind, f, g, node, a, a.save != 0, u);
+    if (!kind_is_adjoint(kind) && a.bcu_out[0]) {
+        a.bcu_out[0][node] = double(u[0]);
+        a.bcu_out[1][node] = double(u[1]);
+        if (PL_LAT::ND == 3) a.bcu_out[2][node] = double(u[2]);
+    }
+    const TC sf = TC(a.ph.shift_f), sg = TC(a.ph.shift_g);
+    store_node<PL_LAT, PL_STORE, true>(static_cast<PL_STORE *>(a.dst), a.geo, node, f, g, sf, sg);
+    (void)Q;
+}
+
+// direct: boundary nodes no smoothing op writes: pull + ops in call order + collide + store
+static __global__ void __launch_bounds__(128) k_bnd_direct(KArgs a, int kind) {
+    constexpr int Q = PL_LAT::Q;
+    const int s = blockIdx.x * 128 + threadIdx.x;
+    if (s >= a.ndir) return;
+    const int node = a.dnode[s];
+    int i, j, k;
+    coords<PL_LAT>(a.geo, node, i, j, k);
+    TC f[Q], g[Q];
+    const TC sf = TC(a.ph.shift_f), sg = TC(a.ph.shift_g);
+    load_node<PL_LAT, PL_STORE, true>(static_cast<const PL_STORE *>(a.src), a.geo, node, i, j, k, a.pull != 0, a.sgn,
+                                      is_interior<PL_LAT>(a.geo, i, j, k), f, g, sf, sg);
+    for (int o = a.dstart[s]; o < a.dstart[s + 1]; ++o) apply_op<PL_LAT, TC>(a.dops[o], f, g, node, a);
+    finish_boundary(kind, f, g, node, a);
+}
+// staged path for the nodes smoothing touches: pre-collision states -> smoothing levels (one
+// launch each, entries of a level independent) -> collide of the targets
+static __global__ void __launch_bounds__(128) k_bnd_pre(KArgs a) {
+    const int s = blockIdx.x * 128 + threadIdx.x;
+    if (s < a.ns) bnd_pre_node<PL_LAT, PL_STORE>(a, s);
+}
+static __global__ void __launch_bounds__(128) k_bnd_smooth(KArgs a, int lo, int hi) {
+    const int e = lo + blockIdx.x * 128 + threadIdx.x;
+    if (e < hi) bnd_smooth_entry<PL_LAT, TC>(a.sent[e], static_cast<TC *>(a.tbuf), a.ns);
+}
+static __global__ void __launch_bounds__(128) k_bnd_post(KArgs a, int kind) {
+    constexpr int Q = PL_LAT::Q;
+    const int t = blockIdx.x * 128 + threadIdx.x;
+    if (t >= a.nt) return;
+    const int s = a.tslot[t];
+    const int idx = a.snode[s];
+    const TC *tb = static_cast<const TC *>(a.tbuf);
+    TC f[Q], g[Q];
+#pragma unroll
+    for (int c = 0; c < Q; ++c) {
+        f[c] = tb[(long long)c * a.ns + s];
+        g[c] = tb[(long long)(Q + c) * a.ns + s];
+    }
+    finish_boundary(kind, f, g, idx, a);
+}
+
 template <int K>
 static void run_kind(int op, bool save, const KArgs &a, cudaStream_t st) {
     const int gi = (a.geo.n + kBlock - 1) / kBlock;
     switch (op) {
     case OP_COLLIDE:
-        if (save) k_interior<PL_LAT, PL_STORE, K, true, false><<<gi, kBlock, 0, st>>>(a);
-        else k_interior<PL_LAT, PL_STORE, K, false, false><<<gi, kBlock, 0, st>>>(a);
+        k_interior<PL_LAT, PL_STORE, K, false><<<gi, kBlock, 0, st>>>(a);
         break;
     case OP_STEP:
-        if (save) k_interior<PL_LAT, PL_STORE, K, true, true><<<gi, kBlock, 0, st>>>(a);
-        else k_interior<PL_LAT, PL_STORE, K, false, true><<<gi, kBlock, 0, st>>>(a);
-        if (a.nb > 0) k_boundary<PL_LAT, PL_STORE, K><<<(a.nb + 127) / 128, 128, 0, st>>>(a);
+        if (a.nb > 0 && a.staged) {
+            // two boundary chains on side streams, concurrent with the interior kernel
+            cudaStream_t side = static_cast<cudaStream_t>(a.side), side2 = static_cast<cudaStream_t>(a.side2);
+            cudaEventRecord(static_cast<cudaEvent_t>(a.ev_fork), st);
+            cudaStreamWaitEvent(side, static_cast<cudaEvent_t>(a.ev_fork), 0);
+            cudaStreamWaitEvent(side2, static_cast<cudaEvent_t>(a.ev_fork), 0);
+            if (a.ndir > 0) k_bnd_direct<<<(a.ndir + 127) / 128, 128, 0, side>>>(a, K);
+            if (a.ns > 0) {
+                k_bnd_pre<<<(a.ns + 127) / 128, 128, 0, side2>>>(a);
+                for (int l = 0; l < a.ngroups; ++l) {
+                    const int lo = a.h_gstart[l], hi = a.h_gstart[l + 1];
+                    if (hi > lo) k_bnd_smooth<<<(hi - lo + 127) / 128, 128, 0, side2>>>(a, lo, hi);
+                }
+                if (a.nt > 0) k_bnd_post<<<(a.nt + 127) / 128, 128, 0, side2>>>(a, K);
+            }
+            k_interior<PL_LAT, PL_STORE, K, true><<<gi, kBlock, 0, st>>>(a);
+            cudaEventRecord(static_cast<cudaEvent_t>(a.ev_join), side);
+            cudaEventRecord(static_cast<cudaEvent_t>(a.ev_join2), side2);
+            cudaStreamWaitEvent(st, static_cast<cudaEvent_t>(a.ev_join), 0);
+            cudaStreamWaitEvent(st, static_cast<cudaEvent_t>(a.ev_join2), 0);
+        } else {
+            k_interior<PL_LAT, PL_STORE, K, true><<<gi, kBlock, 0, st>>>(a);
+            if (a.nb > 0) k_boundary<PL_LAT, PL_STORE, K><<<(a.nb + 127) / 128, 128, 0, st>>>(a);
+        }
         break;
     case OP_BOUNDARY:
         if (a.nb > 0) k_boundary<PL_LAT, PL_STORE, K><<<(a.nb + 127) / 128, 128, 0, st>>>(a);

@@ -67,20 +67,74 @@ __device__ __forceinline__ void store_node(S *__restrict__ dst, const Geo &g, in
 }
 
 // ---- interior kernel --------------------------------------------------------------------
-template <class L, class S, int K, bool SAVE, bool PULL>
-__global__ void __launch_bounds__(kBlock) k_interior(KArgs a) {
+// PULL: stream + boundary program (fused step); otherwise collide in place. With a staged
+// boundary program (a.icode), nodes on a face or flagged carry a code: -2 = handled by the
+// side path (smoothing targets, ops this kind does not apply inline), >= 0 = simple ops applied
+// here, after the pull, in call order (kinds with kind_inline_bc only). Without one, the
+// face mask / flags select the nodes the recursive boundary kernel handles.
+template <class L> __device__ __forceinline__ bool on_face(const Geo &g, int i, int j, int k) {
+    return i == 0 || i == g.nx - 1 || j == 0 || j == g.ny - 1 || (L::ND == 3 && (k == 0 || k == g.nz - 1));
+}
+template <class L, class S, int K, bool PULL>
+__global__ void __launch_bounds__(kBlock, 4) k_interior(KArgs a) {
     using T = typename Store<S>::T;
     constexpr bool HG = kind_has_g(K);
+    constexpr bool INL = kind_inline_bc(K);
     const int idx = blockIdx.x * kBlock + threadIdx.x;
     if (idx >= a.geo.n) return;
     int i, j, k;
     coords<L>(a.geo, idx, i, j, k);
-    if (PULL && skip_boundary<L>(a.geo, idx, i, j, k)) return;
+    int code = -1;
+    if (PULL) {
+        if (a.icode) {
+            const bool cand = a.geo.flags ? a.geo.flags[idx] != 0 : on_face<L>(a.geo, i, j, k);
+            if (cand) code = a.icode[idx];
+            if (code == -2 || (!INL && code >= 0)) return;
+        } else if (skip_boundary<L>(a.geo, idx, i, j, k)) {
+            return;
+        }
+    }
+    // boundary node: its op record, velocity and kappa are fetched alongside the populations
+    InlineRec rec;
+    T up[3] = {T(0), T(0), T(0)}, kp = T(0);
+    if constexpr (PULL && INL) {
+        if (code >= 0) {
+            rec = a.irec[code];
+            if (a.bcu[0]) { up[0] = T(a.bcu[0][idx]); up[1] = T(a.bcu[1][idx]); if (L::ND == 3) up[2] = T(a.bcu[2][idx]); }
+            if (a.bckappa) kp = T(a.bckappa[idx]);
+        }
+    }
     T f[L::Q], g[L::Q];
     const T sf = T(a.ph.shift_f), sg = T(a.ph.shift_g);
     load_node<L, S, HG>(static_cast<const S *>(a.src), a.geo, idx, i, j, k, PULL, K >= 10 ? 1 : -1,
                         is_interior<L>(a.geo, i, j, k), f, g, sf, sg);
-    collide_node<L, T, K>(f, g, idx, a, SAVE, nullptr, a.geo.np, nullptr);
+    if constexpr (PULL && INL) {
+        // only the op application diverges; every lane shares the collide below
+        if (code >= 0) {
+            for (int m = 0; m < (int)rec.nops; ++m) {
+                const uint32_t b = (rec.code >> (8 * m)) & 0xffu;
+                Op op;
+                op.kind = simple_kind(int(b & 7u));
+                op.axis = int8_t((b >> 3) & 3u);
+                op.dir = (b & 32u) ? 1 : -1;
+                op.lat = (b & 64u) ? 1 : 0;
+                op.sub = (b & 128u) ? 2 : 1;
+                op.v0 = rec.v[m];
+                op.v1 = rec.w[m];
+                op.eps = rec.v[m];
+                apply_op<L, T, true>(op, f, g, idx, a, up, kp);
+            }
+        }
+    }
+    T u[3];
+    collide_node<L, T, K>(f, g, idx, a, a.save != 0, nullptr, a.geo.np, (PULL && INL && K < 10) ? u : nullptr);
+    if constexpr (PULL && INL && K < 10) {
+        if (code >= 0 && a.bcu_out[0]) {
+            a.bcu_out[0][idx] = double(u[0]);
+            a.bcu_out[1][idx] = double(u[1]);
+            if (L::ND == 3) a.bcu_out[2][idx] = double(u[2]);
+        }
+    }
     store_node<L, S, HG>(static_cast<S *>(a.dst), a.geo, idx, f, g, sf, sg);
 }
 
@@ -123,7 +177,7 @@ __device__ __noinline__ void eval_node(const KArgs &a, int node, int seq_limit, 
                 for (int c = 0; c < Q; ++c) p[c] = nn == 2 ? T(0.5) * acc[c] : acc[c] / T(3);
             }
         } else {
-            apply_op<L, T>(op, f, g, node, a);
+            apply_op_ni<L, T>(op, f, g, node, a);
         }
     }
 }
@@ -146,6 +200,43 @@ __global__ void __launch_bounds__(128) k_boundary(KArgs a) {
     }
     const T sf = T(a.ph.shift_f), sg = T(a.ph.shift_g);
     store_node<L, S, HG>(static_cast<S *>(a.dst), a.geo, idx, f, g, sf, sg);
+}
+
+// ---- staged boundary path -------------------------------------------------------------------
+// pre-collision state of staged node s: pull + its non-smoothing ops -> scratch
+template <class L, class S>
+__device__ __forceinline__ void bnd_pre_node(const KArgs &a, int s) {
+    using T = typename Store<S>::T;
+    constexpr int Q = L::Q;
+    const int node = a.snode[s];
+    int i, j, k;
+    coords<L>(a.geo, node, i, j, k);
+    T f[Q], g[Q];
+    const T sf = T(a.ph.shift_f), sg = T(a.ph.shift_g);
+    load_node<L, S, true>(static_cast<const S *>(a.src), a.geo, node, i, j, k, a.pull != 0, a.sgn,
+                          is_interior<L>(a.geo, i, j, k), f, g, sf, sg);
+    for (int o = a.sstart[s]; o < a.sstart[s + 1]; ++o) apply_op<L, T>(a.sops[o], f, g, node, a);
+    T *tb = static_cast<T *>(a.tbuf);
+#pragma unroll
+    for (int c = 0; c < Q; ++c) {
+        tb[(long long)c * a.ns + s] = f[c];
+        tb[(long long)(Q + c) * a.ns + s] = g[c];
+    }
+}
+// one smoothing entry: all neighbour values are read before the target is written
+template <class L, class T>
+__device__ __forceinline__ void bnd_smooth_entry(const SmoothEntry &x, T *tb, int nslot) {
+    constexpr int Q = L::Q;
+    const long long base = (long long)x.lat * Q;
+    T v[Q];
+#pragma unroll
+    for (int c = 0; c < Q; ++c) {
+        const T *p = tb + (base + c) * nslot;
+        const T s2 = p[x.nbr[0]] + p[x.nbr[1]];
+        v[c] = x.nnbr == 3 ? (s2 + p[x.nbr[2]]) / T(3) : T(0.5) * s2;
+    }
+#pragma unroll
+    for (int c = 0; c < Q; ++c) tb[(base + c) * nslot + x.slot] = v[c];
 }
 
 // ---- snapshot: the collide's pre-relaxation g (what the reference stores in gi / igi) ----

@@ -399,7 +399,8 @@ def test_solve_matches_driver_loop(o):
     lp.init(0, one, ux=zero, uy=zero, uz=zero)
     lp.init(1, zero, ux=zero, uy=zero, uz=zero)
     prog = lp.program(HS.to_descs(ops))
-    st, steps, res = lp.solve(A.AD_NATURAL, phys(**ph), prog, max_steps=400, check_every=10, tol=1e-3)
+    tol = 2e-3
+    st, steps, res = lp.solve(A.AD_NATURAL, phys(**ph), prog, max_steps=400, check_every=10, tol=tol)
     # oracle driver loop with the same check cadence
     f, g = np.zeros((q, n)), np.zeros((q, n))
     o.init(L, 0, f, o.fields(rho=one, ux=zero, uy=zero, uz=zero))
@@ -412,8 +413,9 @@ def test_solve_matches_driver_loop(o):
         if t % 10 == 0:
             r0 = o.residual([cur["ux"], cur["uy"]], [prev["ux"], prev["uy"]])
             r1 = o.residual([cur["qx"], cur["qy"]], [prev["qx"], prev["qy"]])
-            if r0 < 1e-3 and r1 < 1e-3:
-                ost, osteps, ores = A.PL_CONVERGED, t, (r0, r1)
+            ores = (r0, r1)
+            if r0 < tol and r1 < tol:
+                ost, osteps = A.PL_CONVERGED, t
                 break
         o.stream(L, f)
         o.stream(L, g)
