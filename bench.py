@@ -206,7 +206,8 @@ def main():
     n = p.lx * p.ly * p.lz
     zero, one = np.zeros(n), np.ones(n)
     lp = LatticePair(q, p.lx, p.ly, p.lz, wl["storage"])
-    stream = torch.cuda.current_stream()
+    stream = torch.cuda.Stream()    # a created stream: capturable into the library's CUDA graphs
+    torch.cuda.set_stream(stream)
     lp.set_stream(stream.cuda_stream)
     lp.set_field(A.ALPHA, alpha)
     lp.set_field(A.KAPPA, kappa)

@@ -135,6 +135,14 @@ int pl_synchronize(pl_lattice h);
 /* launch on a caller-owned CUDA stream (a cudaStream_t passed as void*; NULL = legacy default
  * stream) instead of the lattice's own non-blocking stream */
 int pl_set_stream(pl_lattice h, void *stream);
+/* launch options (no counterpart in the reference, which has no launch policy):
+ *  PL_OPT_GRAPHS         1: pl_steps replays a captured two-step CUDA graph; 0 (default):
+ *                        eager launches, which keep the boundary streams' priority
+ *  PL_OPT_SIDE_PRIORITY  1 (default): the boundary chains run on high-priority streams; 0:
+ *                        lowest priority */
+#define PL_OPT_GRAPHS 1
+#define PL_OPT_SIDE_PRIORITY 2
+int pl_set_option(pl_lattice h, int option, int value);
 /* shift of 16-bit population storage, per set (default: f 1.0, g 0.0) */
 int pl_set_shift(pl_lattice h, double shift_f, double shift_g);
 

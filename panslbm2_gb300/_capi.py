@@ -23,6 +23,7 @@ BC_ANS_U, BC_ANS_RHO, BC_AAD_T, BC_AAD_Q, BC_AAD_RHO = 7, 8, 9, 10, 11
 SMOOTH_CORNER, SMOOTH_AT, SMOOTH_LINE = 20, 21, 22
 # fields
 ALPHA, KAPPA, BETA, DIRX, DIRY, DIRZ = 0, 1, 2, 3, 4, 5
+OPT_GRAPHS, OPT_SIDE_PRIORITY = 1, 2
 RHO, UX, UY, UZ, TEM, QX, QY, QZ = 8, 9, 10, 11, 12, 13, 14, 15
 IP, IUX, IUY, IUZ, IMX, IMY, IMZ, ITEM, IQX, IQY, IQZ = 16, 17, 18, 19, 20, 21, 22, 23, 24, 25, 26
 FWD_RHO, FWD_UX, FWD_UY, FWD_UZ, FWD_TEM = 32, 33, 34, 35, 36
@@ -44,7 +45,8 @@ class BcDesc(C.Structure):
 
 
 EXPORTS = [
-    "pl_create", "pl_destroy", "pl_last_error", "pl_synchronize", "pl_set_stream", "pl_set_shift",
+    "pl_create", "pl_destroy", "pl_last_error", "pl_synchronize", "pl_set_stream", "pl_set_option",
+    "pl_set_shift",
     "pl_set_populations", "pl_get_populations", "pl_set_field", "pl_get_field", "pl_freeze_forward",
     "pl_program_create", "pl_program_destroy", "pl_init", "pl_collide", "pl_step", "pl_steps", "pl_stream",
     "pl_solve", "pl_snapshot", "pl_residual", "pl_residual_host", "pl_sensitivity", "pl_heaviside_var",

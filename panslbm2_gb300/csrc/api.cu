@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 #include <stdarg.h>
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
@@ -109,6 +110,16 @@ struct pl_lattice_s {
     long long launches = 0;
     LaunchFn launch = nullptr;
     AuxFn aux = nullptr;
+    // CUDA graphs of two fused steps (one ping-pong period), keyed by the step inputs
+    struct GraphKey {
+        int kind, prog, cur, fwd_next, adj_next, fwd_latest;
+        pl_phys ph;
+        bool operator<(const GraphKey &o) const { return memcmp(this, &o, sizeof *this) < 0; }
+    };
+    struct GraphEntry { cudaGraphExec_t exec; long long launches; };
+    int side_prio = 0, prio_lo = 0, prio_hi = 0;
+    std::map<GraphKey, GraphEntry> graphs;
+    bool use_graphs = true;
 };
 
 namespace {
@@ -373,6 +384,7 @@ int compile_program(pl_lattice h, const pl_bc_desc *descs, int ndesc, Program &P
             bool simple = bstart[sl + 1] - bstart[sl] <= pl::kInlineMaxOps;
             for (int o = bstart[sl]; o < bstart[sl + 1]; ++o)
                 if (!pl::op_is_simple(ops[o].kind)) simple = false;
+
             if (simple) {
                 pl::InlineRec rec;
                 memset(&rec, 0, sizeof rec);
@@ -761,8 +773,12 @@ int pl_create(int q, int nx, int ny, int nz, int storage, pl_lattice *out) {
     // interior kernel frees resources, instead of after its last block has been dispatched
     int prio_lo = 0, prio_hi = 0;
     cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
-    cudaStreamCreateWithPriority(&h->side, cudaStreamNonBlocking, prio_hi);
-    cudaStreamCreateWithPriority(&h->side2, cudaStreamNonBlocking, prio_hi);
+    h->prio_lo = prio_lo;
+    h->prio_hi = prio_hi;
+    h->side_prio = prio_hi;
+    cudaStreamCreateWithPriority(&h->side, cudaStreamNonBlocking, h->side_prio);
+    cudaStreamCreateWithPriority(&h->side2, cudaStreamNonBlocking, h->side_prio);
+    h->use_graphs = false;   // eager launches keep the side-stream priority (faster here)
     cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming);
     cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming);
     cudaEventCreateWithFlags(&h->ev_join2, cudaEventDisableTiming);
@@ -774,6 +790,8 @@ int pl_create(int q, int nx, int ny, int nz, int storage, pl_lattice *out) {
 int pl_destroy(pl_lattice h) {
     if (!h) return PL_OK;
     if (h->st) cudaStreamSynchronize(h->st);
+    for (auto &kv : h->graphs) cudaGraphExecDestroy(kv.second.exec);
+    h->graphs.clear();
     for (auto &P : h->progs) free_program(P);
     for (auto &kv : h->taps) { cudaFree(kv.second.di); cudaFree(kv.second.dj); cudaFree(kv.second.dk); cudaFree(kv.second.hat); }
     cudaFree(h->pop[0]); cudaFree(h->pop[1]);
@@ -810,6 +828,32 @@ int pl_set_stream(pl_lattice h, void *stream) {
     h->st = static_cast<cudaStream_t>(stream);
     h->own_stream = false;
     return PL_OK;
+}
+
+int pl_set_option(pl_lattice h, int option, int value) {
+    if (!h) return fail(PL_ERR_ARG, "null handle");
+    if (value != 0 && value != 1) return fail(PL_ERR_ARG, "option value must be 0 or 1");
+    if (option == PL_OPT_GRAPHS) {
+        h->use_graphs = value == 1;
+        return PL_OK;
+    }
+    if (option == PL_OPT_SIDE_PRIORITY) {
+        const int prio = value ? h->prio_hi : h->prio_lo;
+        if (prio == h->side_prio) return PL_OK;
+        CK(cudaStreamSynchronize(h->st));
+        CK(cudaStreamSynchronize(h->side));
+        CK(cudaStreamSynchronize(h->side2));
+        cudaStreamDestroy(h->side);
+        cudaStreamDestroy(h->side2);
+        h->side = h->side2 = nullptr;
+        CK(cudaStreamCreateWithPriority(&h->side, cudaStreamNonBlocking, prio));
+        CK(cudaStreamCreateWithPriority(&h->side2, cudaStreamNonBlocking, prio));
+        h->side_prio = prio;
+        for (auto &kv : h->graphs) cudaGraphExecDestroy(kv.second.exec);
+        h->graphs.clear();
+        return PL_OK;
+    }
+    return fail(PL_ERR_ARG, "unknown option");
 }
 
 int pl_set_shift(pl_lattice h, double sf, double sg) {
@@ -908,6 +952,10 @@ int pl_program_create(pl_lattice h, const pl_bc_desc *descs, int n, int *prog) {
 int pl_program_destroy(pl_lattice h, int prog) {
     if (!h || prog < 0 || prog >= (int)h->progs.size()) return fail(PL_ERR_ARG, "bad program");
     cudaStreamSynchronize(h->st);
+    for (auto it = h->graphs.begin(); it != h->graphs.end();) {
+        if (it->first.prog == prog) { cudaGraphExecDestroy(it->second.exec); it = h->graphs.erase(it); }
+        else ++it;
+    }
     free_program(h->progs[prog]);
     return PL_OK;
 }
@@ -949,9 +997,73 @@ int pl_step(pl_lattice h, int kind, const pl_phys *ph, int prog, int save) {
 int pl_steps(pl_lattice h, int kind, const pl_phys *ph, int prog, int n) {
     if (!h || !ph || n < 0) return fail(PL_ERR_ARG, "bad arguments");
     CK(cudaEventRecord(h->ev0, h->st));
-    for (int t = 0; t < n; ++t) {
-        int r = do_step(h, kind, ph, prog, false);
-        if (r) return r;
+    int r;
+    // n fused steps without saves. Two steps return every buffer and slot to its parity, so
+    // they are captured once into a CUDA graph and replayed (no per-kernel host launch cost).
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaStreamIsCapturing(h->st, &cs);
+    const bool graphs = h->use_graphs && h->st != nullptr && cs == cudaStreamCaptureStatusNone && n >= 4;
+    int done = 0;
+    if (graphs) {
+        pl_lattice_s::GraphKey key;
+        memset(&key, 0, sizeof key);
+        key.kind = kind; key.prog = prog; key.ph = *ph;
+        for (int warm = 0; warm < 2; ++warm) {   // settle allocations and parity before capture
+            key.cur = h->cur; key.fwd_next = h->fwd_next; key.adj_next = h->adj_next; key.fwd_latest = h->fwd_latest;
+            if (h->graphs.count(key)) break;
+            if ((r = do_step(h, kind, ph, prog, false))) return r;
+            ++done;
+        }
+        key.cur = h->cur; key.fwd_next = h->fwd_next; key.adj_next = h->adj_next; key.fwd_latest = h->fwd_latest;
+        auto it = h->graphs.find(key);
+        if (it == h->graphs.end()) {
+            const long long l0 = h->launches;
+            cudaGraph_t g = nullptr;
+            CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeRelaxed));
+            int rr = do_step(h, kind, ph, prog, false);
+            if (!rr) rr = do_step(h, kind, ph, prog, false);
+            cudaError_t e = cudaStreamEndCapture(h->st, &g);
+            if (rr) { if (g) cudaGraphDestroy(g); return rr; }
+            if (e != cudaSuccess) return fail(PL_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+            // stream priority is not part of a captured launch: give the boundary-chain kernel
+            // nodes (every kernel smaller than the full-lattice grid) the side streams' priority
+            size_t nn = 0;
+            cudaGraphGetNodes(g, nullptr, &nn);
+            std::vector<cudaGraphNode_t> nodes(nn);
+            if (nn) cudaGraphGetNodes(g, nodes.data(), &nn);
+            for (auto nd_ : nodes) {
+                cudaGraphNodeType ty;
+                if (cudaGraphNodeGetType(nd_, &ty) != cudaSuccess || ty != cudaGraphNodeTypeKernel) continue;
+                cudaKernelNodeParams kp;
+                if (cudaGraphKernelNodeGetParams(nd_, &kp) != cudaSuccess) continue;
+                const long long threads = (long long)kp.gridDim.x * kp.blockDim.x;
+                if (threads >= h->n) continue;
+                cudaKernelNodeAttrValue v;
+                memset(&v, 0, sizeof v);
+                v.priority = h->side_prio;
+                cudaGraphKernelNodeSetAttribute(nd_, cudaKernelNodeAttributePriority, &v);
+            }
+            cudaGetLastError();
+            cudaGraphExec_t ex = nullptr;
+            e = cudaGraphInstantiate(&ex, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) return fail(PL_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+            const long long per = h->launches - l0;
+            h->launches = l0;   // captured, not launched: the replays below count them
+            it = h->graphs.emplace(key, pl_lattice_s::GraphEntry{ex, per}).first;
+            // the capture advanced the host state by one period; this first replay runs it
+            CK(cudaGraphLaunch(ex, h->st));
+            h->launches += per;
+            done += 2;
+        }
+        while (n - done >= 2) {
+            CK(cudaGraphLaunch(it->second.exec, h->st));
+            h->launches += it->second.launches;
+            done += 2;
+        }
+    }
+    for (; done < n; ++done) {
+        if ((r = do_step(h, kind, ph, prog, false))) return r;
     }
     CK(cudaEventRecord(h->ev1, h->st));
     return PL_OK;

@@ -318,4 +318,113 @@ __device__ __noinline__ void apply_op_ni(const Op &op, T *f, T *g, int node, con
     apply_op<L, T>(op, f, g, node, a);
 }
 
+// ---- simple ops specialised on the face (axis A, side D) ---------------------------------------
+// Same arithmetic as apply_op; with A and D known at compile time every direction test folds,
+// leaving straight-line code. Used by the interior kernel for boundary nodes.
+template <class L, class T, int A, int D>
+__device__ __forceinline__ void simple_face_op(int sk, int lat, int type, T v0, T v1, T *f, T *g, const T *u, T kp) {
+    constexpr int Q = L::Q, ND = L::ND, NIN = -D;
+    switch (sk) {
+    case 0:   // BC_WALL
+    case 1: { // BC_IWALL
+        T *p = lat ? g : f;
+        T src[Q];
+#pragma unroll
+        for (int c = 0; c < Q; ++c) src[c] = p[c];
+        if (sk == 0) {
+#pragma unroll
+            for (int c = 1; c < Q; ++c)
+                if (comp<L>(c, A) == -D) p[c] = type == 1 ? src[opp<L>(c)] : src[refl<L>(c, A)];
+        } else {
+#pragma unroll
+            for (int c = 1; c < Q; ++c)
+                if (comp<L>(c, A) == D) p[c] = type == 1 ? src[opp<L>(c)] : src[refl<L>(c, A)];
+        }
+        break;
+    }
+    case 2:   // BC_AD_T
+    case 3:   // BC_AD_Q
+    case 4: { // BC_AD_QC
+        T tem0;
+        if (sk == 2) {
+            T s = v0;
+#pragma unroll
+            for (int c = 0; c < Q; ++c) if (comp<L>(c, A) != -D) s -= g[c];
+            tem0 = T(6) * s / (NIN > 0 ? T(1) + T(3) * u[A] : T(1) - T(3) * u[A]);
+        } else {
+            const T kap = sk == 3 ? kp : v1;
+            T s = (T(1) + T(1) / (T(6) * kap)) * v0;
+#pragma unroll
+            for (int c = 1; c < Q; ++c) if (comp<L>(c, A) == D) s += g[c];
+            tem0 = T(6) * s / (NIN > 0 ? T(1) - T(3) * u[A] : T(1) + T(3) * u[A]);
+        }
+#pragma unroll
+        for (int c = 1; c < Q; ++c)
+            if (comp<L>(c, A) == -D) g[c] = tem0 * one_plus_3cu<L, T>(c, u) / inv_w<L, T>(c);
+        break;
+    }
+    case 5:   // BC_AAD_T
+    case 6: { // BC_AAD_Q
+        const T pre = NIN > 0 ? T(1) + T(3) * u[A] : T(1) - T(3) * u[A];
+        const T post = NIN > 0 ? T(1) - T(3) * u[A] : T(1) + T(3) * u[A];
+        T rho0;
+        if (sk == 5) {
+            if (ND == 2) {
+                T num = T(0);
+#pragma unroll
+                for (int c = 1; c < Q; ++c)
+                    if (comp<L>(c, A) == -D && !diag_of<L>(c, A)) num = T(4) * one_plus_3cu<L, T>(c, u) * g[c];
+#pragma unroll
+                for (int c = 1; c < Q; ++c)
+                    if (comp<L>(c, A) == -D && diag_of<L>(c, A)) num += one_plus_3cu<L, T>(c, u) * g[c];
+                rho0 = -num / (T(6) * pre);
+            } else {
+                constexpr int T0 = A == 0 ? 1 : (A == 1 ? 2 : 0), T1 = A == 0 ? 2 : (A == 1 ? 0 : 1);
+                rho0 = -nsum<L, T>(g, A, D, T(8)) / T(12) - u[T0] * tsum<L, T>(g, A, D, T0) / (T(4) * pre)
+                       - u[T1] * tsum<L, T>(g, A, D, T1) / (T(4) * pre);
+            }
+        } else {
+            if (ND == 2) {
+                constexpr int B = 1 - A;
+                const T num = pre * nsum<L, T>(g, A, D, T(4)) + T(3) * u[B] * tsum<L, T>(g, A, D, B) - T(12) * v0;
+                rho0 = num / (T(6) * post);
+            } else {
+                constexpr int T0 = A == 0 ? 1 : (A == 1 ? 2 : 0), T1 = A == 0 ? 2 : (A == 1 ? 0 : 1);
+                constexpr bool K3 = (A == 0 || (A == 1 && D < 0));
+                T num = pre * nsum<L, T>(g, A, D, T(8));
+                if (K3) {
+                    num += T(3) * u[T0] * tsum<L, T>(g, A, D, T0);
+                    num += T(3) * u[T1] * tsum<L, T>(g, A, D, T1);
+                } else {
+                    num += u[T0] * tsum<L, T>(g, A, D, T0);
+                    num += u[T1] * tsum<L, T>(g, A, D, T1);
+                }
+                num -= T(24) * v0;
+                rho0 = num / (T(12) * post);
+            }
+        }
+#pragma unroll
+        for (int c = 1; c < Q; ++c) if (comp<L>(c, A) == D) g[c] = rho0;
+        break;
+    }
+    default:
+        break;
+    }
+}
+
+template <class L, class T>
+__device__ __forceinline__ void simple_op(int axis, int dir, int sk, int lat, int type, T v0, T v1, T *f, T *g,
+                                          const T *u, T kp) {
+    const int face = axis * 2 + (dir > 0 ? 1 : 0);
+    switch (face) {
+    case 0: simple_face_op<L, T, 0, -1>(sk, lat, type, v0, v1, f, g, u, kp); break;
+    case 1: simple_face_op<L, T, 0, 1>(sk, lat, type, v0, v1, f, g, u, kp); break;
+    case 2: simple_face_op<L, T, 1, -1>(sk, lat, type, v0, v1, f, g, u, kp); break;
+    case 3: simple_face_op<L, T, 1, 1>(sk, lat, type, v0, v1, f, g, u, kp); break;
+    case 4: if (L::ND == 3) simple_face_op<L, T, 2, -1>(sk, lat, type, v0, v1, f, g, u, kp); break;
+    case 5: if (L::ND == 3) simple_face_op<L, T, 2, 1>(sk, lat, type, v0, v1, f, g, u, kp); break;
+    default: break;
+    }
+}
+
 }  // namespace pl

@@ -80,7 +80,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_interior(KArgs a) {
     using T = typename Store<S>::T;
     constexpr bool HG = kind_has_g(K);
     constexpr bool INL = kind_inline_bc(K);
-    const int idx = blockIdx.x * kBlock + threadIdx.x;
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= a.geo.n) return;
     int i, j, k;
     coords<L>(a.geo, idx, i, j, k);
@@ -113,16 +113,8 @@ __global__ void __launch_bounds__(kBlock, 4) k_interior(KArgs a) {
         if (code >= 0) {
             for (int m = 0; m < (int)rec.nops; ++m) {
                 const uint32_t b = (rec.code >> (8 * m)) & 0xffu;
-                Op op;
-                op.kind = simple_kind(int(b & 7u));
-                op.axis = int8_t((b >> 3) & 3u);
-                op.dir = (b & 32u) ? 1 : -1;
-                op.lat = (b & 64u) ? 1 : 0;
-                op.sub = (b & 128u) ? 2 : 1;
-                op.v0 = rec.v[m];
-                op.v1 = rec.w[m];
-                op.eps = rec.v[m];
-                apply_op<L, T, true>(op, f, g, idx, a, up, kp);
+                simple_op<L, T>(int((b >> 3) & 3u), (b & 32u) ? 1 : -1, int(b & 7u), (b & 64u) ? 1 : 0,
+                                (b & 128u) ? 2 : 1, T(rec.v[m]), T(rec.w[m]), f, g, up, kp);
             }
         }
     }

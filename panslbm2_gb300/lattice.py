@@ -91,6 +91,9 @@ class LatticePair:
     def set_stream(self, stream_ptr):
         check(self.lib.pl_set_stream(self.h, C.c_void_p(stream_ptr)))
 
+    def set_option(self, option, value):
+        check(self.lib.pl_set_option(self.h, C.c_int(option), C.c_int(int(value))))
+
     def set_shift(self, sf, sg):
         check(self.lib.pl_set_shift(self.h, C.c_double(sf), C.c_double(sg)))
 

@@ -423,3 +423,34 @@ def test_solve_matches_driver_loop(o):
         cur, prev = prev, cur
     assert (st, steps) == (ost, osteps)
     assert abs(res[0] - ores[0]) <= 1e-9 * ores[0] and abs(res[1] - ores[1]) <= 1e-9 * ores[1]
+
+
+@pytest.mark.parametrize("q", [9, 15])
+@pytest.mark.parametrize("n", [4, 7, 12])
+def test_graph_steps_equal_eager_steps(o, q, n):
+    """pl_steps replays a captured two-step CUDA graph; it must equal n eager pl_step calls."""
+    p = _heatsink_case(q)
+    ss = np.clip(HS.grf_design(p.nd, p.lx, p.ly, p.lz, seed=5, sigma=2.0), 0, 1)
+    alpha, kappa, _, _ = p.design_fields(ss)
+    nn = p.lx * p.ly * p.lz
+    one, zero = np.ones(nn), np.zeros(nn)
+    ph = phys(nu=p.nu, diff=0.0, gx=p.gx, gy=p.gy, gz=p.gz, tem0=p.tem0)
+    out = []
+    for graph in (True, False):
+        lp = LatticePair(q, p.lx, p.ly, p.lz, "fp32")
+        lp.set_option(A.OPT_GRAPHS, graph)
+        lp.set_field(A.ALPHA, alpha)
+        lp.set_field(A.KAPPA, kappa)
+        lp.init(0, one, ux=zero, uy=zero, uz=zero)
+        lp.init(1, 0.1 * one, ux=zero, uy=zero, uz=zero)
+        prog = lp.program(HS.to_descs(HS.program_ops("forward", p)))
+        lp.collide(A.AD_NATURAL, ph)
+        if graph:
+            lp.steps(A.AD_NATURAL, ph, prog, n)
+            lp.steps(A.AD_NATURAL, ph, prog, n)      # replays the cached graph
+        else:
+            for _ in range(2 * n):
+                lp.step(A.AD_NATURAL, ph, prog, save=False)
+        out.append((lp.get_populations(0), lp.get_populations(1)))
+        lp.close()
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
