@@ -17,8 +17,8 @@ buffers (2 x 245 MB) exceed the 129 MB L2, so no flush is needed between steps.
   cpu_baseline the C restatement of the reference's scalar OpenMP path (oracle/), FP64, on
                the host cores, on a bounded number of steps of the same workload
 
---impl reference times that CPU path alone (the reference's own implementation of the path
-cannot be built on the GPU host).
+--impl reference times that CPU path alone: the reference's own implementation of the path is
+header-only C++ whose sources are not present on the GPU host, so the restatement stands in.
 """
 import argparse
 import json

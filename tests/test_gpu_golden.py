@@ -1,0 +1,215 @@
+"""The CUDA library (FP64 storage and compute, through the C ABI) against the golden fixtures
+the reference itself produced (tests/golden/*.npz). Stream, walls and smoothing move data
+only and must agree bit for bit; every other output agrees to 1e-12 relative to the field's
+largest magnitude (FP64 kernels compiled without FMA contraction, same evaluation order;
+reductions in the filters and residual use a fixed tree whose summation order differs).
+
+The standalone sensitivity cases feed arbitrary snapshots, which the library only takes from its
+own collides; the sensitivities are checked through hsadj_* (forward, adjoint, snapshots and
+the four sensitivity routines on one handle)."""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from panslbm2_gb300 import _capi as A
+from panslbm2_gb300 import heatsink as HS
+from panslbm2_gb300.lattice import LatticePair, phys
+from tests.golden import cases as C
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+RTOL = 1e-12
+
+
+def _files(prefix):
+    fs = sorted(glob.glob(os.path.join(HERE, "golden", prefix + "_*.npz")))
+    return pytest.mark.parametrize("path", fs, ids=[os.path.basename(f)[:-4] for f in fs])
+
+
+def close(a, b, rtol=RTOL):
+    a, b = np.asarray(a, np.float64).reshape(-1), np.asarray(b, np.float64).reshape(-1)
+    scale = max(1.0, float(np.max(np.abs(b)))) if b.size else 1.0
+    err = float(np.max(np.abs(a - b))) / scale if b.size else 0.0
+    assert err <= rtol, "max rel err %.3e" % err
+
+
+def lattice(inp):
+    q, nx, ny, nz = C._shape(inp)
+    return LatticePair(q, nx, ny, nz, "fp64"), q, nx * ny * nz
+
+
+@_files("stream")
+def test_stream(path):
+    inp, out = C.load(path)
+    lp, q, n = lattice(inp)
+    lp.set_populations(0, inp["f"])
+    lp.set_populations(1, inp["f"])
+    lp.stream(mode=int(inp["inverse"]), both=False)
+    assert np.array_equal(lp.get_populations(0), out["f"])
+    lp.close()
+
+
+@_files("bc")
+def test_boundary_kind(path):
+    inp, out = C.load(path)
+    lp, q, n = lattice(inp)
+    kind = C.BC_KINDS[int(inp["kind"])]
+    adjoint_inputs = kind in ("AAD_T", "AAD_Q", "AAD_RHO")
+    lp.set_populations(0, inp["f"])
+    lp.set_populations(1, inp["g"])
+    lp.set_field(A.KAPPA, inp["kap"])
+    if adjoint_inputs:
+        for fid, nm in ((A.FWD_RHO, "rho"), (A.FWD_UX, "ux"), (A.FWD_UY, "uy"), (A.FWD_UZ, "uz"), (A.FWD_TEM, "tem")):
+            lp.set_field(fid, inp[nm])
+    else:
+        for fid, nm in ((A.UX, "ux"), (A.UY, "uy"), (A.UZ, "uz")):
+            lp.set_field(fid, inp[nm])
+    prog = lp.program(HS.to_descs(C.bc_ops(inp)))
+    lp.stream(mode=3 if adjoint_inputs else 2, prog=prog, both=True)
+    f, g = lp.get_populations(0), lp.get_populations(1)
+    if kind in ("WALL", "IWALL"):
+        assert np.array_equal(f, out["f"]) and np.array_equal(g, out["g"])
+    else:
+        close(f, out["f"])
+        close(g, out["g"])
+    lp.close()
+
+
+@_files("smooth")
+def test_smoothing(path):
+    inp, out = C.load(path)
+    lp, q, n = lattice(inp)
+    lp.set_populations(0, inp["f"])
+    lp.set_populations(1, inp["g"])
+    lp.stream(mode=2, prog=lp.program(HS.to_descs(C.smooth_ops(q))), both=True)
+    assert np.array_equal(lp.get_populations(0), out["f"])
+    assert np.array_equal(lp.get_populations(1), out["g"])
+    lp.close()
+
+
+@_files("collide")
+def test_collide(path):
+    inp, out = C.load(path)
+    lp, q, n = lattice(inp)
+    k = int(inp["kind"])
+    lp.set_populations(0, inp["f"])
+    if inp["g"].size:
+        lp.set_populations(1, inp["g"])
+    for fid, nm in ((A.ALPHA, "alpha"), (A.KAPPA, "diffusivity"), (A.BETA, "beta"), (A.DIRX, "dirx"),
+                    (A.DIRY, "diry"), (A.DIRZ, "dirz")):
+        lp.set_field(fid, inp[nm])
+    if k >= 10:
+        for fid, nm in ((A.FWD_RHO, "rho"), (A.FWD_UX, "ux"), (A.FWD_UY, "uy"), (A.FWD_UZ, "uz"), (A.FWD_TEM, "tem")):
+            lp.set_field(fid, inp[nm])
+    lp.collide(k, phys(**C.PH), save=True)
+    close(lp.get_populations(0), out["f"])
+    if inp["g"].size:
+        close(lp.get_populations(1), out["g"])
+    names, base = (C.ADJ_NAMES, A.IP) if k >= 10 else (C.FWD_NAMES, A.RHO)
+    for m, nm in enumerate(names):
+        if q == 9 and nm.endswith("z"):
+            continue
+        if not inp["g"].size and nm in ("tem", "qx", "qy", "qz", "item", "iqx", "iqy", "iqz"):
+            continue
+        if k == A.AAD_FORCE and nm == "iuz":
+            continue     # not saved by the reference's 3D routine (its output array stays as it was)
+        close(lp.get_field(base + m), out["m_" + nm], 1e-11)
+    if k in (A.AD_NATURAL, A.AD_FORCE, A.AAD_NATURAL, A.AAD_FORCE, A.AAD_MASSFLOW):
+        close(lp.snapshot(1 if k >= 10 else 0), out["snap"])
+    lp.close()
+
+
+@_files("init")
+def test_initial_condition(path):
+    inp, out = C.load(path)
+    lp, q, n = lattice(inp)
+    w = int(inp["which"])
+    a = {0: ("rho",), 1: ("tem",), 2: ("ip", "iux", "iuy", "iuz"), 3: ("item", "iqx", "iqy", "iqz")}[w]
+    args = [inp[nm] for nm in a]
+    lp.init(w, *args, ux=inp["ux"], uy=inp["uy"], uz=inp["uz"])
+    close(lp.get_populations(0 if w in (0, 2) else 1), out["f"])
+    lp.close()
+
+
+@_files("filter")
+def test_filters(path):
+    inp, out = C.load(path)
+    lp, q, n = lattice(inp)
+    R, beta = float(inp["R"]), float(inp["beta"])
+    mask = inp["mask"] if inp["mask"].size else None
+    close(lp.heaviside_var(R, beta, inp["s"], mask), out["var"])
+    close(lp.heaviside_sens(R, beta, inp["s"], inp["dfd"], mask), out["sens"])
+    close(lp.density_filter(R, inp["s"], mask), out["dens"])
+    lp.close()
+
+
+@_files("resid")
+def test_residual_normalize(path):
+    inp, out = C.load(path)
+    lp = LatticePair(9, 40, 40, 1, "fp64")
+    nc = int(inp["ncomp"])
+    r = lp.residual_host([inp["a%d" % m] for m in range(nc)], [inp["b%d" % m] for m in range(nc)])
+    assert abs(r - float(out["residual"])) <= RTOL * abs(float(out["residual"]))
+    assert np.array_equal(lp.normalize(inp["a0"].copy()), out["normalized"])
+    lp.close()
+
+
+def _forward(inp):
+    p = C.hs_params("q9" if int(inp["sk"]) == 0 else "q15")
+    q = 9 if p.nd == 2 else 15
+    lp = LatticePair(q, p.lx, p.ly, p.lz, "fp64")
+    lp.set_field(A.ALPHA, inp["alpha"])
+    lp.set_field(A.KAPPA, inp["kappa"])
+    lp.init(0, inp["rho0"], ux=inp["ux0"], uy=inp["uy0"], uz=inp["uz0"])
+    lp.init(1, inp["tem0"], ux=inp["ux0"], uy=inp["uy0"], uz=inp["uz0"])
+    ph = phys(**C.hs_phys(p))
+    prog = lp.program(HS.to_descs(HS.program_ops("forward", p)))
+    lp.collide(A.AD_NATURAL, ph, save=True)
+    for t in range(2, C.HS_FWD_STEPS + 1):
+        lp.step(A.AD_NATURAL, ph, prog, save=(t == C.HS_FWD_STEPS))
+    return lp, p, q, ph
+
+
+@_files("hsfwd")
+def test_heatsink_forward(path):
+    inp, out = C.load(path)
+    lp, p, q, _ = _forward(inp)
+    close(lp.get_populations(0), out["f"], 1e-11)
+    close(lp.get_populations(1), out["g"], 1e-11)
+    for m, nm in enumerate(C.FWD_NAMES):
+        if q == 9 and nm.endswith("z"):
+            continue
+        close(lp.get_field(A.RHO + m), out["m_" + nm], 1e-11)
+    close(lp.snapshot(0), out["snap"], 1e-11)
+    lp.close()
+
+
+@_files("hsadj")
+def test_heatsink_adjoint_and_sensitivities(path):
+    inp, out = C.load(path)
+    lp, p, q, ph = _forward(inp)
+    lp.snapshot(0, host=False)
+    lp.freeze_forward()
+    fu = [lp.get_field(A.FWD_UX), lp.get_field(A.FWD_UY), lp.get_field(A.FWD_UZ)]
+    lp.init(2, inp["ip0"], inp["iux0"], inp["iuy0"], inp["iuz0"], ux=fu[0], uy=fu[1], uz=fu[2])
+    lp.init(3, inp["it0"], inp["iqx0"], inp["iqy0"], inp["iqz0"], ux=fu[0], uy=fu[1], uz=fu[2])
+    prog = lp.program(HS.to_descs(HS.program_ops("adjoint", p)))
+    lp.collide(A.AAD_NATURAL, ph, save=True)
+    for t in range(2, C.HS_ADJ_STEPS + 1):
+        lp.step(A.AAD_NATURAL, ph, prog, save=(t == C.HS_ADJ_STEPS))
+    close(lp.get_populations(0), out["f"], 1e-11)
+    close(lp.get_populations(1), out["g"], 1e-11)
+    for m, nm in enumerate(C.ADJ_NAMES):
+        if q == 9 and nm.endswith("z"):
+            continue
+        close(lp.get_field(A.IP + m), out["m_" + nm], 1e-11)
+    close(lp.snapshot(1), out["snap"], 1e-11)
+    qn, mask = p.source()
+    n = lp.n
+    for which in range(4):
+        got = lp.sensitivity(which, np.zeros(n), inp["dads"], inp["dkds"], qn, mask)
+        close(got, out["sens%d" % which], 1e-10)
+    lp.close()
