@@ -193,6 +193,16 @@ int pl_snapshot(pl_lattice h, int slot, double *host);
 int pl_residual(pl_lattice h, int family, double *out);
 /* Residual of arbitrary host arrays (ncomp of a, ncomp of b, n each) */
 int pl_residual_host(pl_lattice h, int n, int ncomp, const double *const *a, const double *const *b, double *out);
+/* Residual of caller-owned DEVICE arrays (a[m], b[m]: n doubles each, m < ncomp <= 3) on
+ * `stream` (a cudaStream_t as void*, NULL = legacy default stream); *out = sqrt(sum (a-b)^2 /
+ * sum a^2), the same value pl_residual_host gives. No counterpart in the reference (its
+ * Residual runs on host arrays). Allocates nothing: its scratch is a fixed 16 KB device array
+ * in the library, shared by all calls on a device. The first call on each device looks that
+ * array up (make it before any stream capture on the device); calls from several host threads
+ * that can overlap on the GPU race on it and must be serialised. Returns after the result has
+ * been copied to *out. */
+int pl_residual_device_noalloc(long long n, int ncomp, const double *const *a, const double *const *b, void *stream,
+                               double *out);
 
 /* sensitivities (dfds host array of N, accumulated into like the reference):
  * which 0 AAD::SensitivityTemperatureAtHeatSource (adjointadvection.h:1495-1543, qn/mask per node)

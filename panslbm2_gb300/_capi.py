@@ -10,6 +10,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libpanslbm_gb300.so")
 
 PL_OK = 0
+PL_ERR_ARG, PL_ERR_CUDA, PL_ERR_UNSUPPORTED, PL_ERR_STATE, PL_ERR_ALLOC, PL_ERR_NONFINITE = -1, -2, -3, -4, -5, -6
 PL_CONVERGED, PL_MAX_STEPS, PL_DIVERGED = 1, 2, 3
 PL_FP64, PL_FP32, PL_FP16, PL_BF16 = 0, 1, 2, 3
 STORAGE = {"fp64": PL_FP64, "fp32": PL_FP32, "fp16": PL_FP16, "bf16": PL_BF16}
@@ -49,7 +50,8 @@ EXPORTS = [
     "pl_set_shift",
     "pl_set_populations", "pl_get_populations", "pl_set_field", "pl_get_field", "pl_freeze_forward",
     "pl_program_create", "pl_program_destroy", "pl_init", "pl_collide", "pl_step", "pl_steps", "pl_stream",
-    "pl_solve", "pl_snapshot", "pl_residual", "pl_residual_host", "pl_sensitivity", "pl_heaviside_var",
+    "pl_solve", "pl_snapshot", "pl_residual", "pl_residual_host", "pl_residual_device_noalloc",
+    "pl_sensitivity", "pl_heaviside_var",
     "pl_heaviside_sens", "pl_density_filter", "pl_normalize", "pl_stats",
 ]
 

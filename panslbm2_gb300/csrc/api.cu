@@ -723,6 +723,8 @@ int scratch(pl_lattice h, int i, double **p) {
 }  // namespace
 
 // ==================================================================================== C ABI
+int pl::record_error(int code, const char *msg) { return fail(code, "%s", msg); }
+
 extern "C" {
 
 const char *pl_last_error(void) { return g_err.c_str(); }

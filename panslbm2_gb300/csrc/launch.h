@@ -20,4 +20,7 @@ PL_DECL(d3q15_f32)
 PL_DECL(d3q15_f16)
 PL_DECL(d3q15_bf16)
 #undef PL_DECL
+
+// records the message pl_last_error returns (for entry points defined outside api.cu)
+int record_error(int code, const char *msg);
 }  // namespace pl
