@@ -114,12 +114,16 @@ def peaks():
 
 def traffic_per_node(workload):
     """DRAM bytes per node of the fused step from the committed ncu summary, if any."""
-    path = os.path.join(ROOT, "profiles", "step_traffic.json")
+    path = os.path.join(ROOT, "profiles", "step_traffic.txt")
     try:
         with open(path) as fh:
-            return json.load(fh).get(workload)
-    except Exception:
-        return None
+            for line in fh:
+                parts = line.split()
+                if len(parts) == 2 and parts[0] == workload:
+                    return float(parts[1])
+    except OSError:
+        pass
+    return None
 
 
 def cpu_port(p, alpha, kappa, ops, q, budget_s=12.0, max_steps=30):

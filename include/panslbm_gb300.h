@@ -187,6 +187,9 @@ int pl_solve(pl_lattice h, int kind, const pl_phys *ph, int prog, int max_steps,
  * slot 0 forward, 1 adjoint; host may be NULL (kept on the device for pl_sensitivity).
  * host layout: snap[q*idx + c] (the reference's scalar layout). */
 int pl_snapshot(pl_lattice h, int slot, double *host);
+/* load a snapshot slot from a host array in the same layout (a gi / igi the caller kept, e.g.
+ * one per time step of a transient sweep) for the next pl_sensitivity */
+int pl_set_snapshot(pl_lattice h, int slot, const double *host);
 
 /* Residual(...) of residual.h over the current (a) and previous (b) saved macros:
  * family 0 = (ux,uy[,uz]), 1 = (qx,qy[,qz]), 2 = (iux,iuy[,iuz]), 3 = (iqx,iqy[,iqz]). */

@@ -50,7 +50,7 @@ EXPORTS = [
     "pl_set_shift",
     "pl_set_populations", "pl_get_populations", "pl_set_field", "pl_get_field", "pl_freeze_forward",
     "pl_program_create", "pl_program_destroy", "pl_init", "pl_collide", "pl_step", "pl_steps", "pl_stream",
-    "pl_solve", "pl_snapshot", "pl_residual", "pl_residual_host", "pl_residual_device_noalloc",
+    "pl_solve", "pl_snapshot", "pl_set_snapshot", "pl_residual", "pl_residual_host", "pl_residual_device_noalloc",
     "pl_sensitivity", "pl_heaviside_var",
     "pl_heaviside_sens", "pl_density_filter", "pl_normalize", "pl_stats",
 ]

@@ -1161,6 +1161,17 @@ int pl_snapshot(pl_lattice h, int slot, double *host) {
     return PL_OK;
 }
 
+int pl_set_snapshot(pl_lattice h, int slot, const double *host) {
+    if (!h || !host || (slot != 0 && slot != 1)) return fail(PL_ERR_ARG, "bad arguments");
+    int r = ensure_d(h, &h->snap[slot], (size_t)h->q * h->np);
+    if (r) return r;
+    double *buf;
+    if ((r = scratch(h, 2, &buf))) return r;
+    if ((r = upload(h, buf, host, (size_t)h->q * h->n))) return r;
+    pl::launch_node_major_to_snap(buf, h->np, h->n, h->q, h->snap[slot], h->st);
+    return check_launch(h, 1);
+}
+
 int pl_residual(pl_lattice h, int family, double *out) {
     if (!h || !out || family < 0 || family > 3) return fail(PL_ERR_ARG, "bad arguments");
     double o[3];

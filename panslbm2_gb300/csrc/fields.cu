@@ -249,5 +249,15 @@ void launch_snap_to_node_major(const double *snap, long long np, int n, int q, d
     const long long tot = (long long)n * q;
     k_transpose_snap<<<(unsigned)((tot + kRB - 1) / kRB), kRB, 0, st>>>(snap, np, n, q, out);
 }
+__global__ void k_untranspose_snap(const double *in, long long np, int n, int q, double *snap) {
+    const long long t = (long long)blockIdx.x * kRB + threadIdx.x;
+    if (t >= (long long)n * q) return;
+    const int idx = int(t / q), c = int(t % q);
+    snap[(long long)c * np + idx] = in[t];
+}
+void launch_node_major_to_snap(const double *in, long long np, int n, int q, double *snap, cudaStream_t st) {
+    const long long tot = (long long)n * q;
+    k_untranspose_snap<<<(unsigned)((tot + kRB - 1) / kRB), kRB, 0, st>>>(in, np, n, q, snap);
+}
 
 }  // namespace pl

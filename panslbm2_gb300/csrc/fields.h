@@ -41,5 +41,6 @@ void launch_filter(int op, const FiltArgs &f, const double *a, const double *b, 
                    cudaStream_t st);
 void launch_to_compute(const double *in, void *out, int n, bool fp32, cudaStream_t st);
 void launch_snap_to_node_major(const double *snap, long long np, int n, int q, double *out, cudaStream_t st);
+void launch_node_major_to_snap(const double *in, long long np, int n, int q, double *snap, cudaStream_t st);
 
 }  // namespace pl

@@ -174,6 +174,10 @@ class LatticePair:
         check(self.lib.pl_snapshot(self.h, slot, _dp(out)))
         return out
 
+    def set_snapshot(self, slot, snap):
+        snap = _f64(snap, self.n * self.q)
+        check(self.lib.pl_set_snapshot(self.h, slot, _dp(snap)))
+
     def residual(self, family):
         out = C.c_double()
         check(self.lib.pl_residual(self.h, family, C.byref(out)))

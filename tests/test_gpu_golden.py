@@ -191,7 +191,7 @@ def test_heatsink_forward(path):
 def test_heatsink_adjoint_and_sensitivities(path):
     inp, out = C.load(path)
     lp, p, q, ph = _forward(inp)
-    lp.snapshot(0, host=False)
+    g0 = lp.snapshot(0)                 # also kept on the device for the sensitivity
     lp.freeze_forward()
     fu = [lp.get_field(A.FWD_UX), lp.get_field(A.FWD_UY), lp.get_field(A.FWD_UZ)]
     lp.init(2, inp["ip0"], inp["iux0"], inp["iuy0"], inp["iuz0"], ux=fu[0], uy=fu[1], uz=fu[2])
@@ -206,10 +206,17 @@ def test_heatsink_adjoint_and_sensitivities(path):
         if q == 9 and nm.endswith("z"):
             continue
         close(lp.get_field(A.IP + m), out["m_" + nm], 1e-11)
-    close(lp.snapshot(1), out["snap"], 1e-11)
+    g1 = lp.snapshot(1)
+    close(g1, out["snap"], 1e-11)
     qn, mask = p.source()
     n = lp.n
+    got = []
     for which in range(4):
-        got = lp.sensitivity(which, np.zeros(n), inp["dads"], inp["dkds"], qn, mask)
-        close(got, out["sens%d" % which], 1e-10)
+        got.append(lp.sensitivity(which, np.zeros(n), inp["dads"], inp["dkds"], qn, mask))
+        close(got[-1], out["sens%d" % which], 1e-10)
+    # the same sensitivities from snapshots loaded back from host copies (pl_set_snapshot)
+    lp.set_snapshot(0, g0)
+    lp.set_snapshot(1, g1)
+    for which in range(2):
+        assert np.array_equal(lp.sensitivity(which, np.zeros(n), inp["dads"], inp["dkds"], qn, mask), got[which])
     lp.close()
