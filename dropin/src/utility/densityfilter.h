@@ -1,0 +1,28 @@
+//  densityfilter.h -- drop-in DensityFilter (utility/densityfilter.h:10-515 of the reference):
+//  the weighted average of radius R on the device. The weight functor has the form described in
+//  heavisidefilter.h.
+#pragma once
+#include <vector>
+#include "../gpu/runtime.h"
+
+namespace PANSLBM2 {
+    namespace DensityFilter {
+        template<class T, template<class>class P, class F>
+        std::vector<T> GetFilteredValue(P<T>& _p, T _R, const std::vector<T> &_v, F _weight) {
+            gpu::Pair &pr = *_p.gpu_particle().pair;
+            const std::vector<int> &mask = gpu::filter_mask(pr, double(_R), _weight);
+            std::vector<double> v(_v.begin(), _v.end()), out(pr.n);
+            gpu::ck(pl_density_filter(pr.h, double(_R), v.data(), mask.empty() ? nullptr : mask.data(), out.data()),
+                    "pl_density_filter");
+            return std::vector<T>(out.begin(), out.end());
+        }
+
+        template<class T, template<class>class P>
+        std::vector<T> GetFilteredValue(P<T>& _p, T _R, const std::vector<T> &_v) {
+            gpu::Pair &pr = *_p.gpu_particle().pair;
+            std::vector<double> v(_v.begin(), _v.end()), out(pr.n);
+            gpu::ck(pl_density_filter(pr.h, double(_R), v.data(), nullptr, out.data()), "pl_density_filter");
+            return std::vector<T>(out.begin(), out.end());
+        }
+    }
+}

@@ -1,0 +1,50 @@
+//  heavisidefilter.h -- drop-in HeavisideFilter (utility/heavisidefilter.h:404-899 of the
+//  reference): the density filter of radius R followed by the Heaviside projection (beta,
+//  threshold 0.5), and the chain rule of its sensitivity, on the device.
+//
+//  The weight functor must have the reference drivers' form: the hat weight (R - distance) / R,
+//  everywhere or between two nodes of a design region with the identity elsewhere. Its region
+//  is inferred and checked against the functor on every tap (gpu::filter_mask).
+#pragma once
+#include <vector>
+#include "../gpu/runtime.h"
+
+namespace PANSLBM2 {
+    namespace HeavisideFilter {
+        template<class T, template<class>class P, class F>
+        std::vector<T> GetFilteredVariable(P<T>& _p, T _R, T _beta, const std::vector<T> &_s, F _weight) {
+            gpu::Pair &pr = *_p.gpu_particle().pair;
+            const std::vector<int> &mask = gpu::filter_mask(pr, double(_R), _weight);
+            std::vector<double> s(_s.begin(), _s.end()), out(pr.n);
+            gpu::ck(pl_heaviside_var(pr.h, double(_R), double(_beta), s.data(), mask.empty() ? nullptr : mask.data(), out.data()),
+                    "pl_heaviside_var");
+            return std::vector<T>(out.begin(), out.end());
+        }
+
+        template<class T, template<class>class P>
+        std::vector<T> GetFilteredVariable(P<T>& _p, T _R, T _beta, const std::vector<T> &_s) {
+            gpu::Pair &pr = *_p.gpu_particle().pair;
+            std::vector<double> s(_s.begin(), _s.end()), out(pr.n);
+            gpu::ck(pl_heaviside_var(pr.h, double(_R), double(_beta), s.data(), nullptr, out.data()), "pl_heaviside_var");
+            return std::vector<T>(out.begin(), out.end());
+        }
+
+        template<class T, template<class>class P, class F>
+        std::vector<T> GetFilteredSensitivity(P<T>& _p, T _R, T _beta, const std::vector<T> &_s, const std::vector<T> &_dfdrho, F _weight) {
+            gpu::Pair &pr = *_p.gpu_particle().pair;
+            const std::vector<int> &mask = gpu::filter_mask(pr, double(_R), _weight);
+            std::vector<double> s(_s.begin(), _s.end()), d(_dfdrho.begin(), _dfdrho.end()), out(pr.n);
+            gpu::ck(pl_heaviside_sens(pr.h, double(_R), double(_beta), s.data(), d.data(), mask.empty() ? nullptr : mask.data(),
+                                      out.data()), "pl_heaviside_sens");
+            return std::vector<T>(out.begin(), out.end());
+        }
+
+        template<class T, template<class>class P>
+        std::vector<T> GetFilteredSensitivity(P<T>& _p, T _R, T _beta, const std::vector<T> &_s, const std::vector<T> &_dfdrho) {
+            gpu::Pair &pr = *_p.gpu_particle().pair;
+            std::vector<double> s(_s.begin(), _s.end()), d(_dfdrho.begin(), _dfdrho.end()), out(pr.n);
+            gpu::ck(pl_heaviside_sens(pr.h, double(_R), double(_beta), s.data(), d.data(), nullptr, out.data()), "pl_heaviside_sens");
+            return std::vector<T>(out.begin(), out.end());
+        }
+    }
+}

@@ -3,10 +3,10 @@
  *
  * The reference (PANSLBM2) is a header-only C++ template library with no FFI; its
  * "interface" is the set of template functions the production drivers call. Each entry point
- * below replaces one group of those calls; the C++ template layer in dropin/ (same header
- * paths, namespaces and signatures as the reference) forwards to these symbols, and any other
- * host language binds them directly. All pointers named `host*` are host
- * memory; device memory is owned by the library and never crosses this boundary.
+ * below replaces one group of those calls. The C++ template layer in dropin/src (the
+ * reference's header paths, namespaces and signatures) is built on these symbols; other host
+ * languages bind them directly. All pointers named `host*` are host memory; device memory is
+ * owned by the library and never crosses this boundary (pl_residual_device_noalloc excepted).
  *
  * Every call returns PL_OK (0) or a negative error code; pl_last_error() describes the last
  * failure of the calling thread. Calls are asynchronous on the lattice's CUDA stream except
