@@ -55,9 +55,8 @@ struct Program {
     int *dnode = nullptr, *dstart = nullptr, *snode = nullptr, *sstart = nullptr, *tslot = nullptr;
     int *dnode_all = nullptr, *dstart_all = nullptr;
     Op *dops = nullptr, *sops = nullptr, *dops_all = nullptr;
-    pl::SmoothEntry *sent = nullptr;
-    std::vector<int> gstart;
-    int *d_gstart = nullptr;
+    pl::SmoothNode *sexpr = nullptr;  // composed smoothing averages
+    int *troot = nullptr;             // per target and set: average or scratch slot
     void *tbuf = nullptr;
 };
 
@@ -355,12 +354,29 @@ int compile_program(pl_lattice h, const pl_bc_desc *descs, int ndesc, Program &P
         if (last_plain[o.node] > first_smooth[o.node]) staged = false;
         for (int m = 0; m < o.sub; ++m) if (last_plain[o.nbr[m]] > o.seq) staged = false;
     }
+    {
+        // ... and when the composed smoothing averages nest no deeper than the device evaluates
+        std::vector<const Op *> sm;
+        for (const Op &o : ops) if (o.kind == pl::BC_SMOOTH) sm.push_back(&o);
+        std::stable_sort(sm.begin(), sm.end(), [](const Op *x, const Op *y) { return x->seq < y->seq; });
+        std::map<long long, int> depth;   // (set, node) -> nesting of its current value
+        for (const Op *o : sm) {
+            int d = 0;
+            for (int m = 0; m < o->sub; ++m) {
+                auto it = depth.find((long long)o->lat * h->n + o->nbr[m]);
+                if (it != depth.end()) d = std::max(d, it->second);
+            }
+            depth[(long long)o->lat * h->n + o->node] = d + 1;
+            if (d + 1 > pl::kSmoothDepth) staged = false;
+        }
+    }
     // direct set D (boundary nodes no smoothing op writes), staged set S (nodes smoothing reads
     // or writes), targets T (nodes smoothing writes)
     std::vector<int> dnode, dstart, snode, sstart, tslot, dnode_all, dstart_all, icode;
     std::vector<pl::InlineRec> irec;
     std::vector<Op> dops, sops, dops_all;
-    std::vector<pl::SmoothEntry> sent;
+    std::vector<pl::SmoothNode> sexpr;
+    std::vector<int> troot;
     if (staged) {
         std::vector<char> is_t(h->n, 0), is_s(h->n, 0);
         for (const Op &o : ops)
@@ -415,31 +431,24 @@ int compile_program(pl_lattice h, const pl_bc_desc *descs, int ndesc, Program &P
             if (is_s[node]) { sslot[node] = (int)snode.size(); snode.push_back(node); sstart.push_back((int)sops.size()); plain_ops(node, sops); }
         sstart.push_back((int)sops.size());
         for (int node = 0; node < h->n; ++node) if (is_t[node]) tslot.push_back(sslot[node]);
-        // smoothing ops in call order, scheduled into dependency levels (per population set:
-        // read-after-write, write-after-read and write-after-write order is kept)
+        // smoothing ops in call order, composed into one expression per (target, set): a
+        // node's current value is its pre-smoothing scratch slot until an average writes it
         std::vector<const Op *> sm;
         for (const Op &o : ops) if (o.kind == pl::BC_SMOOTH) sm.push_back(&o);
         std::stable_sort(sm.begin(), sm.end(), [](const Op *x, const Op *y) { return x->seq < y->seq; });
         const size_t NS = snode.size();
-        std::vector<int> lw(2 * NS, 0), lr(2 * NS, 0);
-        std::vector<std::vector<pl::SmoothEntry>> lev;
+        std::vector<int> cur(2 * NS);
+        for (size_t sl = 0; sl < NS; ++sl) cur[sl] = cur[NS + sl] = -(int)sl - 1;
         for (const Op *o : sm) {
             const size_t L0 = o->lat ? NS : 0;
-            const int self = sslot[o->node];
-            int lvl = std::max(lw[L0 + self], lr[L0 + self]);
-            for (int m = 0; m < o->sub; ++m) lvl = std::max(lvl, lw[L0 + sslot[o->nbr[m]]]);
-            lvl += 1;
-            lw[L0 + self] = lvl;
-            for (int m = 0; m < o->sub; ++m) lr[L0 + sslot[o->nbr[m]]] = std::max(lr[L0 + sslot[o->nbr[m]]], lvl);
-            if ((int)lev.size() < lvl) lev.resize(lvl);
-            pl::SmoothEntry e;
-            memset(&e, 0, sizeof e);
-            e.slot = self; e.lat = o->lat; e.nnbr = (int8_t)o->sub;
-            for (int m = 0; m < 3; ++m) e.nbr[m] = m < o->sub ? sslot[o->nbr[m]] : 0;
-            lev[lvl - 1].push_back(e);
+            pl::SmoothNode x;
+            memset(&x, 0, sizeof x);
+            x.nnbr = o->sub;
+            for (int m = 0; m < o->sub; ++m) x.child[m] = cur[L0 + sslot[o->nbr[m]]];
+            sexpr.push_back(x);
+            cur[L0 + sslot[o->node]] = (int)sexpr.size() - 1;
         }
-        P.gstart.assign(1, 0);
-        for (auto &l : lev) { sent.insert(sent.end(), l.begin(), l.end()); P.gstart.push_back((int)sent.size()); }
+        for (int sl : tslot) { troot.push_back(cur[sl]); troot.push_back(cur[NS + sl]); }
         P.ndir = (int)dnode.size(); P.ndir_all = (int)dnode_all.size(); P.ns = (int)snode.size(); P.nt = (int)tslot.size();
     }
     P.staged = staged;
@@ -481,12 +490,12 @@ int compile_program(pl_lattice h, const pl_bc_desc *descs, int ndesc, Program &P
             if ((r = dalloc((void **)&P.irec, sizeof(pl::InlineRec) * irec.size()))) return r;
             CK(cudaMemcpyAsync(P.irec, irec.data(), sizeof(pl::InlineRec) * irec.size(), cudaMemcpyHostToDevice, h->st));
         }
-        if (!sent.empty()) {
-            if ((r = dalloc((void **)&P.sent, sizeof(pl::SmoothEntry) * sent.size()))) return r;
-            CK(cudaMemcpyAsync(P.sent, sent.data(), sizeof(pl::SmoothEntry) * sent.size(), cudaMemcpyHostToDevice, h->st));
+        if (!sexpr.empty()) {
+            if ((r = dalloc((void **)&P.sexpr, sizeof(pl::SmoothNode) * sexpr.size()))) return r;
+            CK(cudaMemcpyAsync(P.sexpr, sexpr.data(), sizeof(pl::SmoothNode) * sexpr.size(), cudaMemcpyHostToDevice, h->st));
         }
         if (P.ns && (r = dalloc(&P.tbuf, h->csize * 2 * h->q * (size_t)P.ns))) return r;
-        if ((r = up_i(&P.d_gstart, P.gstart))) return r;
+        if ((r = up_i(&P.troot, troot))) return r;
     }
     if (!geometric) {
         if ((r = dalloc((void **)&P.flags, h->n))) return r;
@@ -500,7 +509,7 @@ int compile_program(pl_lattice h, const pl_bc_desc *descs, int ndesc, Program &P
 void free_program(Program &P) {
     cudaFree(P.bnode); cudaFree(P.bstart); cudaFree(P.slot_of); cudaFree(P.ops); cudaFree(P.flags);
     cudaFree(P.dnode); cudaFree(P.dstart); cudaFree(P.snode); cudaFree(P.sstart); cudaFree(P.tslot);
-    cudaFree(P.dops); cudaFree(P.sops); cudaFree(P.sent); cudaFree(P.tbuf); cudaFree(P.d_gstart);
+    cudaFree(P.dops); cudaFree(P.sops); cudaFree(P.sexpr); cudaFree(P.tbuf); cudaFree(P.troot);
     cudaFree(P.icode); cudaFree(P.irec); cudaFree(P.dnode_all); cudaFree(P.dstart_all); cudaFree(P.dops_all);
     P = Program();
 }
@@ -578,9 +587,7 @@ program:
         if (pl::kind_inline_bc(kind) && kind_inputs) { a.ndir = P.ndir; a.dnode = P.dnode; a.dstart = P.dstart; a.dops = P.dops; }
         else { a.ndir = P.ndir_all; a.dnode = P.dnode_all; a.dstart = P.dstart_all; a.dops = P.dops_all; }
         a.snode = P.snode; a.sstart = P.sstart; a.sops = P.sops; a.tslot = P.tslot;
-        a.sent = P.sent; a.tbuf = P.tbuf;
-        a.h_gstart = P.gstart.data(); a.gstart = P.d_gstart;
-        a.ngroups = P.gstart.empty() ? 0 : (int)P.gstart.size() - 1;
+        a.sexpr = P.sexpr; a.troot = P.troot; a.tbuf = P.tbuf;
         a.side = h->side; a.side2 = h->side2; a.ev_fork = h->ev_fork; a.ev_join = h->ev_join; a.ev_join2 = h->ev_join2;
         // velocity read by AD/AAD ops
         if (!adjk) {
@@ -644,7 +651,7 @@ int do_step(pl_lattice h, int kind, const pl_phys *ph, int prog, bool save) {
     int r = build_args(h, kind, ph, prog, h->cur, h->cur ^ 1, save, true, bcu_slot, a);
     if (r) return r;
     if (h->launch(kind, pl::OP_STEP, save, a, h->st)) return fail(PL_ERR_UNSUPPORTED, "kind %d not built for this storage", kind);
-    if ((r = check_launch(h, a.nb > 0 ? (a.staged ? 1 + (a.ndir > 0) + (a.ns > 0 ? 2 + a.ngroups : 0) : 2) : 1))) return r;
+    if ((r = check_launch(h, a.nb > 0 ? (a.staged ? 1 + (a.ndir > 0) + (a.ns > 0 ? 2 : 0) : 2) : 1))) return r;
     after_collide(h, kind, save, h->cur, prog, true, bcu_slot, ph);
     h->cur ^= 1;
     return PL_OK;

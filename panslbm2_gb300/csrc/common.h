@@ -66,12 +66,15 @@ struct Op {
     double v0, v1, v2, eps;
 };
 
-// One smoothing update of the staged boundary path: node `slot` of set `lat` becomes the mean
-// of nnbr neighbour slots (all indices into the boundary scratch buffer).
-struct SmoothEntry {
-    int32_t slot, nbr[3];
-    int8_t lat, nnbr, pad[2];
+// One smoothing average of the staged boundary path: the mean of nnbr operands, each either
+// another average (child >= 0: its index) or the pre-smoothing value of a boundary-scratch slot
+// (child < 0: slot -child-1). The smoothing calls of a step compose, in call order, into one
+// such expression per (target, population set).
+struct SmoothNode {
+    int32_t child[3];
+    int32_t nnbr;
 };
+constexpr int kSmoothDepth = 8;   // deepest composition the device evaluates
 
 struct Geo {
     int nx, ny, nz, n;    // lattice extents, node count
@@ -115,10 +118,8 @@ struct KArgs {
     const Op *dops;
     const int *snode, *sstart, *tslot;
     const Op *sops;
-    const SmoothEntry *sent;    // smoothing entries, grouped by level (slots index snode)
-    const int *gstart;          // entry offsets of the levels (ngroups+1), device
-    const int *h_gstart;        // the same offsets, host
-    int ngroups;
+    const SmoothNode *sexpr;    // smoothing averages
+    const int *troot;           // per target t and set: troot[2t+lat] >= 0 average, < 0 slot -v-1
     void *tbuf;                 // scratch: 2*Q planes of ns compute-type values
     void *side, *side2;         // host: cudaStream_t of the two boundary chains
     void *ev_fork, *ev_join, *ev_join2;   // host: cudaEvent_t
@@ -129,6 +130,6 @@ struct KArgs {
     int *err;                   // device error word (bit flags)
 };
 
-enum ErrBits { ERR_RECURSION = 1, ERR_BAD_OP = 2 };
+enum ErrBits { ERR_RECURSION = 1, ERR_BAD_OP = 2, ERR_SMOOTH_DEPTH = 4 };
 
 }  // namespace pl

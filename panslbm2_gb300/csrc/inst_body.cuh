@@ -61,38 +61,48 @@ static __global__ void __launch_bounds__(128) k_bnd_direct(KArgs a, int kind) {
     for (int o = a.dstart[s]; o < a.dstart[s + 1]; ++o) apply_op<PL_LAT, TC>(a.dops[o], f, g, node, a);
     finish_boundary(kind, f, g, node, a);
 }
-// staged path for the nodes smoothing touches: pre-collision states -> smoothing levels (one
-// launch each, entries of a level independent) -> collide of the targets
+// staged path for the nodes smoothing touches: pre-collision states into scratch (pre), then
+// per target the composed smoothing expressions, the collide and the store (post)
 static __global__ void __launch_bounds__(128) k_bnd_pre(KArgs a) {
     const int s = blockIdx.x * 128 + threadIdx.x;
     if (s < a.ns) bnd_pre_node<PL_LAT, PL_STORE>(a, s);
-}
-static __global__ void __launch_bounds__(128) k_bnd_smooth(KArgs a, int lo, int hi) {
-    const int e = lo + blockIdx.x * 128 + threadIdx.x;
-    if (e < hi) bnd_smooth_entry<PL_LAT, TC>(a.sent[e], static_cast<TC *>(a.tbuf), a.ns);
 }
 static __global__ void __launch_bounds__(128) k_bnd_post(KArgs a, int kind) {
     constexpr int Q = PL_LAT::Q;
     const int t = blockIdx.x * 128 + threadIdx.x;
     if (t >= a.nt) return;
-    const int s = a.tslot[t];
-    const int idx = a.snode[s];
+    const int idx = a.snode[a.tslot[t]];
     const TC *tb = static_cast<const TC *>(a.tbuf);
     TC f[Q], g[Q];
+#pragma unroll 1
+    for (int lat = 0; lat < 2; ++lat) {
+        const int root = a.troot[2 * t + lat];
+        TC *dst = lat ? g : f;
 #pragma unroll
-    for (int c = 0; c < Q; ++c) {
-        f[c] = tb[(long long)c * a.ns + s];
-        g[c] = tb[(long long)(Q + c) * a.ns + s];
+        for (int c = 0; c < Q; ++c) {
+            const long long plane = (long long)lat * Q + c;
+            dst[c] = root < 0 ? tb[plane * a.ns + (-root - 1)]
+                              : smooth_eval<TC, kSmoothDepth>(a.sexpr, root, tb, plane, a.ns, a.err);
+        }
     }
     finish_boundary(kind, f, g, idx, a);
 }
 
+static dim3 interior_grid(const Geo &g) {
+    return dim3((g.nx + 31) / 32, (g.ny + 7) / 8, PL_LAT::ND == 2 ? 1 : g.nz);
+}
+
+// the pull part of a fused step
+template <int K>
+static void launch_pull(const KArgs &a, cudaStream_t st) {
+    k_interior<PL_LAT, PL_STORE, K, true><<<interior_grid(a.geo), dim3(32, 8), 0, st>>>(a);
+}
+
 template <int K>
 static void run_kind(int op, bool save, const KArgs &a, cudaStream_t st) {
-    const int gi = (a.geo.n + kBlock - 1) / kBlock;
     switch (op) {
     case OP_COLLIDE:
-        k_interior<PL_LAT, PL_STORE, K, false><<<gi, kBlock, 0, st>>>(a);
+        k_interior<PL_LAT, PL_STORE, K, false><<<interior_grid(a.geo), dim3(32, 8), 0, st>>>(a);
         break;
     case OP_STEP:
         if (a.nb > 0 && a.staged) {
@@ -104,19 +114,15 @@ static void run_kind(int op, bool save, const KArgs &a, cudaStream_t st) {
             if (a.ndir > 0) k_bnd_direct<<<(a.ndir + 127) / 128, 128, 0, side>>>(a, K);
             if (a.ns > 0) {
                 k_bnd_pre<<<(a.ns + 127) / 128, 128, 0, side2>>>(a);
-                for (int l = 0; l < a.ngroups; ++l) {
-                    const int lo = a.h_gstart[l], hi = a.h_gstart[l + 1];
-                    if (hi > lo) k_bnd_smooth<<<(hi - lo + 127) / 128, 128, 0, side2>>>(a, lo, hi);
-                }
                 if (a.nt > 0) k_bnd_post<<<(a.nt + 127) / 128, 128, 0, side2>>>(a, K);
             }
-            k_interior<PL_LAT, PL_STORE, K, true><<<gi, kBlock, 0, st>>>(a);
+            launch_pull<K>(a, st);
             cudaEventRecord(static_cast<cudaEvent_t>(a.ev_join), side);
             cudaEventRecord(static_cast<cudaEvent_t>(a.ev_join2), side2);
             cudaStreamWaitEvent(st, static_cast<cudaEvent_t>(a.ev_join), 0);
             cudaStreamWaitEvent(st, static_cast<cudaEvent_t>(a.ev_join2), 0);
         } else {
-            k_interior<PL_LAT, PL_STORE, K, true><<<gi, kBlock, 0, st>>>(a);
+            launch_pull<K>(a, st);
             if (a.nb > 0) k_boundary<PL_LAT, PL_STORE, K><<<(a.nb + 127) / 128, 128, 0, st>>>(a);
         }
         break;

@@ -75,15 +75,56 @@ __device__ __forceinline__ void store_node(S *__restrict__ dst, const Geo &g, in
 template <class L> __device__ __forceinline__ bool on_face(const Geo &g, int i, int j, int k) {
     return i == 0 || i == g.nx - 1 || j == 0 || j == g.ny - 1 || (L::ND == 3 && (k == 0 || k == g.nz - 1));
 }
+// After the pull: the node's inline boundary ops, the collide, the boundary velocity the next
+// step's ops read, and the store. Only the op application diverges; every lane of a warp
+// shares the collide.
+template <class L, class S, int K>
+__device__ __forceinline__ void node_tail(const KArgs &a, int idx, int code, typename Store<S>::T *f,
+                                          typename Store<S>::T *g, typename Store<S>::T sf,
+                                          typename Store<S>::T sg) {
+    using T = typename Store<S>::T;
+    constexpr bool HG = kind_has_g(K);
+    constexpr bool INL = kind_inline_bc(K);
+    if constexpr (INL) {
+        if (code >= 0) {
+            const InlineRec &rec = a.irec[code];
+            T up[3] = {T(0), T(0), T(0)}, kp = T(0);
+            if (a.bcu[0]) { up[0] = T(a.bcu[0][idx]); up[1] = T(a.bcu[1][idx]); if (L::ND == 3) up[2] = T(a.bcu[2][idx]); }
+            if (a.bckappa) kp = T(a.bckappa[idx]);
+            const uint32_t code8 = rec.code, nops = rec.nops;
+            for (int m = 0; m < (int)nops; ++m) {
+                const uint32_t b = (code8 >> (8 * m)) & 0xffu;
+                simple_op<L, T>(int((b >> 3) & 3u), (b & 32u) ? 1 : -1, int(b & 7u), (b & 64u) ? 1 : 0,
+                                (b & 128u) ? 2 : 1, T(rec.v[m]), T(rec.w[m]), f, g, up, kp);
+            }
+        }
+    }
+    T u[3];
+    collide_node<L, T, K>(f, g, idx, a, a.save != 0, nullptr, a.geo.np, (INL && K < 10) ? u : nullptr);
+    if constexpr (INL && K < 10) {
+        if (code >= 0 && a.bcu_out[0]) {
+            a.bcu_out[0][idx] = double(u[0]);
+            a.bcu_out[1][idx] = double(u[1]);
+            if (L::ND == 3) a.bcu_out[2][idx] = double(u[2]);
+        }
+    }
+    store_node<L, S, HG>(static_cast<S *>(a.dst), a.geo, idx, f, g, sf, sg);
+}
+
+// Launched on a (ceil(nx/32), ceil(ny/8), nz) grid of 32 x 8 blocks: lane = x within a 32-node
+// tile (128-byte aligned accesses), warp = row; coordinates come from the block and thread
+// indices. (Moving the x-face nodes into warps of their own was measured slower: it splits the
+// 32-byte sectors at x = 0 and x = nx - 1 between two warps' stores.)
 template <class L, class S, int K, bool PULL>
 __global__ void __launch_bounds__(kBlock, 4) k_interior(KArgs a) {
     using T = typename Store<S>::T;
     constexpr bool HG = kind_has_g(K);
     constexpr bool INL = kind_inline_bc(K);
-    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= a.geo.n) return;
-    int i, j, k;
-    coords<L>(a.geo, idx, i, j, k);
+    const int nx = a.geo.nx;
+    const int i = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y * 8 + threadIdx.y;
+    if (i >= nx || j >= a.geo.ny) return;
+    const int k = blockIdx.z;
+    const int idx = i + nx * (j + a.geo.ny * k);
     int code = -1;
     if (PULL) {
         if (a.icode) {
@@ -94,40 +135,11 @@ __global__ void __launch_bounds__(kBlock, 4) k_interior(KArgs a) {
             return;
         }
     }
-    // boundary node: its op record, velocity and kappa are fetched alongside the populations
-    InlineRec rec;
-    T up[3] = {T(0), T(0), T(0)}, kp = T(0);
-    if constexpr (PULL && INL) {
-        if (code >= 0) {
-            rec = a.irec[code];
-            if (a.bcu[0]) { up[0] = T(a.bcu[0][idx]); up[1] = T(a.bcu[1][idx]); if (L::ND == 3) up[2] = T(a.bcu[2][idx]); }
-            if (a.bckappa) kp = T(a.bckappa[idx]);
-        }
-    }
     T f[L::Q], g[L::Q];
     const T sf = T(a.ph.shift_f), sg = T(a.ph.shift_g);
     load_node<L, S, HG>(static_cast<const S *>(a.src), a.geo, idx, i, j, k, PULL, K >= 10 ? 1 : -1,
                         is_interior<L>(a.geo, i, j, k), f, g, sf, sg);
-    if constexpr (PULL && INL) {
-        // only the op application diverges; every lane shares the collide below
-        if (code >= 0) {
-            for (int m = 0; m < (int)rec.nops; ++m) {
-                const uint32_t b = (rec.code >> (8 * m)) & 0xffu;
-                simple_op<L, T>(int((b >> 3) & 3u), (b & 32u) ? 1 : -1, int(b & 7u), (b & 64u) ? 1 : 0,
-                                (b & 128u) ? 2 : 1, T(rec.v[m]), T(rec.w[m]), f, g, up, kp);
-            }
-        }
-    }
-    T u[3];
-    collide_node<L, T, K>(f, g, idx, a, a.save != 0, nullptr, a.geo.np, (PULL && INL && K < 10) ? u : nullptr);
-    if constexpr (PULL && INL && K < 10) {
-        if (code >= 0 && a.bcu_out[0]) {
-            a.bcu_out[0][idx] = double(u[0]);
-            a.bcu_out[1][idx] = double(u[1]);
-            if (L::ND == 3) a.bcu_out[2][idx] = double(u[2]);
-        }
-    }
-    store_node<L, S, HG>(static_cast<S *>(a.dst), a.geo, idx, f, g, sf, sg);
+    node_tail<L, S, K>(a, idx, PULL ? code : -1, f, g, sf, sg);
 }
 
 // ---- boundary program replay ----------------------------------------------------------------
@@ -215,20 +227,25 @@ __device__ __forceinline__ void bnd_pre_node(const KArgs &a, int s) {
         tb[(long long)(Q + c) * a.ns + s] = g[c];
     }
 }
-// one smoothing entry: all neighbour values are read before the target is written
-template <class L, class T>
-__device__ __forceinline__ void bnd_smooth_entry(const SmoothEntry &x, T *tb, int nslot) {
-    constexpr int Q = L::Q;
-    const long long base = (long long)x.lat * Q;
-    T v[Q];
+// value of population plane `plane` under smoothing expression e: the reference's averages,
+// (a + b) * 0.5 and (a + b + c) / 3 with operands in call order
+template <class T, int D>
+__device__ __noinline__ T smooth_eval(const SmoothNode *ex, int e, const T *tb, long long plane, int nslot, int *err) {
+    if constexpr (D == 0) {
+        atomicOr(err, ERR_SMOOTH_DEPTH);
+        return T(0);
+    } else {
+        const SmoothNode x = ex[e];
+        T v[3];
 #pragma unroll
-    for (int c = 0; c < Q; ++c) {
-        const T *p = tb + (base + c) * nslot;
-        const T s2 = p[x.nbr[0]] + p[x.nbr[1]];
-        v[c] = x.nnbr == 3 ? (s2 + p[x.nbr[2]]) / T(3) : T(0.5) * s2;
+        for (int m = 0; m < 3; ++m) {
+            if (m >= x.nnbr) { v[m] = T(0); continue; }
+            const int ch = x.child[m];
+            v[m] = ch < 0 ? tb[plane * nslot + (-ch - 1)] : smooth_eval<T, D - 1>(ex, ch, tb, plane, nslot, err);
+        }
+        const T s2 = v[0] + v[1];
+        return x.nnbr == 3 ? (s2 + v[2]) / T(3) : T(0.5) * s2;
     }
-#pragma unroll
-    for (int c = 0; c < Q; ++c) tb[(base + c) * nslot + x.slot] = v[c];
 }
 
 // ---- snapshot: the collide's pre-relaxation g (what the reference stores in gi / igi) ----
