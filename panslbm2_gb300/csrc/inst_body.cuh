@@ -67,25 +67,31 @@ static __global__ void __launch_bounds__(128) k_bnd_pre(KArgs a) {
     const int s = blockIdx.x * 128 + threadIdx.x;
     if (s < a.ns) bnd_pre_node<PL_LAT, PL_STORE>(a, s);
 }
-static __global__ void __launch_bounds__(128) k_bnd_post(KArgs a, int kind) {
+// one warp per target: lane l < 2Q evaluates the smoothing expression of set l / Q, population
+// l % Q; lane 0 then collides and stores the target
+constexpr int kPostWarps = 4;
+static __global__ void __launch_bounds__(32 * kPostWarps) k_bnd_post(KArgs a, int kind) {
     constexpr int Q = PL_LAT::Q;
-    const int t = blockIdx.x * 128 + threadIdx.x;
+    __shared__ TC val[kPostWarps][2 * Q];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int t = blockIdx.x * kPostWarps + w;
     if (t >= a.nt) return;
     const int idx = a.snode[a.tslot[t]];
     const TC *tb = static_cast<const TC *>(a.tbuf);
-    TC f[Q], g[Q];
-#pragma unroll 1
-    for (int lat = 0; lat < 2; ++lat) {
+    if (lane < 2 * Q) {
+        const int lat = lane / Q;
         const int root = a.troot[2 * t + lat];
-        TC *dst = lat ? g : f;
-#pragma unroll
-        for (int c = 0; c < Q; ++c) {
-            const long long plane = (long long)lat * Q + c;
-            dst[c] = root < 0 ? tb[plane * a.ns + (-root - 1)]
-                              : smooth_eval<TC, kSmoothDepth>(a.sexpr, root, tb, plane, a.ns, a.err);
-        }
+        const long long plane = lane;   // = lat * Q + c
+        val[w][lane] = root < 0 ? tb[plane * a.ns + (-root - 1)]
+                                : smooth_eval<TC, kSmoothDepth>(a.sexpr, root, tb, plane, a.ns, a.err);
     }
-    finish_boundary(kind, f, g, idx, a);
+    __syncwarp();
+    if (lane == 0) {
+        TC f[Q], g[Q];
+#pragma unroll
+        for (int c = 0; c < Q; ++c) { f[c] = val[w][c]; g[c] = val[w][Q + c]; }
+        finish_boundary(kind, f, g, idx, a);
+    }
 }
 
 static dim3 interior_grid(const Geo &g) {
@@ -114,7 +120,7 @@ static void run_kind(int op, bool save, const KArgs &a, cudaStream_t st) {
             if (a.ndir > 0) k_bnd_direct<<<(a.ndir + 127) / 128, 128, 0, side>>>(a, K);
             if (a.ns > 0) {
                 k_bnd_pre<<<(a.ns + 127) / 128, 128, 0, side2>>>(a);
-                if (a.nt > 0) k_bnd_post<<<(a.nt + 127) / 128, 128, 0, side2>>>(a, K);
+                if (a.nt > 0) k_bnd_post<<<(a.nt + kPostWarps - 1) / kPostWarps, 32 * kPostWarps, 0, side2>>>(a, K);
             }
             launch_pull<K>(a, st);
             cudaEventRecord(static_cast<cudaEvent_t>(a.ev_join), side);
