@@ -16,6 +16,9 @@ buffers (2 x 245 MB) exceed the 129 MB L2, so no flush is needed between steps.
                populations, read alpha and kappa) / measured step time, vs MEASURED_PEAKS
   cpu_baseline the C restatement of the reference's scalar OpenMP path (oracle/), FP64, on
                the host cores, on a bounded number of steps of the same workload
+  design_iter  seconds of one heat-sink design iteration (filter, forward and adjoint to residual
+               1e-6, sensitivity, filtered sensitivity) on the 200x100 FP64 lattice, with the
+               oracle port's time for the same step counts
 
 --impl reference times that CPU path alone: the reference's own implementation of the path is
 header-only C++ whose sources are not present on the GPU host, so the restatement stands in.
@@ -162,6 +165,66 @@ def cpu_port(p, alpha, kappa, ops, q, budget_s=12.0, max_steps=30):
                       % (steps, p.lx, p.ly, p.lz)}
 
 
+DESIGN_LATTICE = dict(nd=2, lx=200, ly=100, lz=1, storage="fp64")
+
+
+def design_gpu(tol=1e-6, max_steps=100000):
+    """One heat-sink design iteration (filter, forward and adjoint to `tol`, sensitivity, filtered
+    and normalised sensitivity) through the library, on the 200x100 FP64 lattice."""
+    from panslbm2_gb300 import heatsink as HS
+    from panslbm2_gb300.design import HeatSinkDesign
+    d = DESIGN_LATTICE
+    p = HS.Params(d["nd"], d["lx"], d["ly"], d["lz"])
+    s = HS.grf_design(d["nd"], d["lx"], d["ly"], d["lz"], seed=0, sigma=8.0)
+    hs = HeatSinkDesign(p, d["storage"])
+    hs.iterate(s, tol=tol, max_steps=2000)          # warm-up: builds the filter taps and programs
+    r = hs.iterate(s, tol=tol, max_steps=max_steps)
+    hs.close()
+    return p, s, r
+
+
+def design_cpu_per_step(p, budget_s=8.0):
+    """Seconds per forward and per adjoint time step of the oracle port (FP64, all host cores) on
+    the design lattice, from a bounded sample of steps with the drivers' every-step saves."""
+    from oracle.olib import Oracle
+    from panslbm2_gb300 import _capi as A
+    from panslbm2_gb300 import heatsink as HS
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from _replay import replay
+    o = Oracle("oracle")
+    o.set_threads(os.cpu_count() or 1)
+    q = 9 if p.nd == 2 else 15
+    L = o.lat(q, p.lx, p.ly, p.lz)
+    n = p.lx * p.ly * p.lz
+    ss = HS.grf_design(p.nd, p.lx, p.ly, p.lz, seed=0, sigma=8.0)
+    alpha, kappa, _, _ = p.design_fields(ss)
+    ph = dict(nu=p.nu, diff=0.0, gx=p.gx, gy=p.gy, gz=p.gz, tem0=p.tem0)
+    out = {}
+    for phase, kind, inverse in (("forward", A.AD_NATURAL, False), ("adjoint", A.AAD_NATURAL, True)):
+        f, g = np.zeros((q, n)), np.zeros((q, n))
+        zero = np.zeros(n)
+        o.init(L, 0, f, o.fields(rho=np.ones(n), ux=zero, uy=zero, uz=zero))
+        o.init(L, 1, g, o.fields(tem=zero, ux=zero, uy=zero, uz=zero))
+        names = ("rho", "ux", "uy", "uz", "tem", "qx", "qy", "qz", "ip", "iux", "iuy", "iuz", "imx", "imy", "imz",
+                 "item", "iqx", "iqy", "iqz")
+        mac = {k: np.zeros(n) for k in names}
+        mac["rho"][:] = 1.0
+        snap = np.zeros(n * q)
+        ops = HS.program_ops(phase, p)
+        F = o.fields(gsnap=snap, alpha=alpha, diffusivity=kappa, **mac)
+        steps, t0 = 0, time.perf_counter()
+        while time.perf_counter() - t0 < budget_s and steps < 2000:
+            o.collide(L, kind, f, g, F, **ph, save=True)
+            o.stream(L, f, inverse)
+            o.stream(L, g, inverse)
+            replay(o, L, f, g, ops, n, ux=mac["ux"], uy=mac["uy"], uz=mac["uz"], rho=mac["rho"], tem=mac["tem"],
+                   kappa=kappa)
+            steps += 1
+        out[phase] = (time.perf_counter() - t0) / max(1, steps)
+        out[phase + "_sample"] = steps
+    return out
+
+
 def run_reference(args, wl):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -187,6 +250,7 @@ def main():
     ap.add_argument("--workload", default=DEFAULT, choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--no-design", action="store_true", help="skip the design-iteration timing")
     args = ap.parse_args()
     wl = WORKLOADS[args.workload]
     if args.impl == "reference":
@@ -282,6 +346,22 @@ def main():
             "config": {"workload": args.workload, "nodes": n, "storage": wl["storage"], "parallelism": "replicas",
                        "l2": "inputs larger than L2: two population buffers of %.0f MB each" % pop_mb},
             "roofline": roof, "e2e": e2e, "clocks": ck, "gpu_launches": int(l1 - l0)}
+    if rank == 0 and not args.no_design:
+        dp, _, r = design_gpu()
+        di = {"lattice": "heatsink2d-200x100-fp64", "tol": 1e-6, "max_steps": 100000,
+              "seconds": round(r["seconds"]["total"], 4),
+              "phases_s": {k: round(v, 4) for k, v in r["seconds"].items()},
+              "forward_steps": r["forward"][1], "adjoint_steps": r["adjoint"][1],
+              "converged": [r["forward"][0] == A.PL_CONVERGED, r["adjoint"][0] == A.PL_CONVERGED],
+              "objective": r["objective"],
+              "what": "filter, forward and adjoint to residual 1e-6 (checked every 100 steps), heat-source "
+                      "sensitivity, filtered and normalised sensitivity; from rest; no MMA update"}
+        if not args.no_cpu:
+            cs = design_cpu_per_step(dp)
+            di["cpu_seconds_est"] = round(cs["forward"] * r["forward"][1] + cs["adjoint"] * r["adjoint"][1], 2)
+            di["cpu_sample"] = ("oracle port, FP64, %d host threads: %d forward and %d adjoint steps timed, scaled to the "
+                                "GPU's step counts" % (os.cpu_count() or 1, cs["forward_sample"], cs["adjoint_sample"]))
+        line["design_iter"] = di
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_port(p, alpha, kappa, ops, q)
     if rank == 0:

@@ -1,0 +1,38 @@
+"""A design iteration on the device (panslbm2_gb300.design): the adjoint heat-source sensitivity
+against central finite differences of the heat-source temperature objective, as the reference's
+crosscheck drivers compare them.
+
+The adjoint of AAD::SensitivityTemperatureAtHeatSource is the gradient of the source-temperature
+functional up to one constant factor (the drivers normalise the sensitivity before the design
+update, so only its direction is used). The test therefore requires the ratio adjoint / FD to be
+the same at every probed cell, within 2% (measured on GB300: within 0.5%)."""
+import numpy as np
+import pytest
+
+from panslbm2_gb300 import heatsink as HS
+from panslbm2_gb300.design import HeatSinkDesign
+
+pytestmark = pytest.mark.gpu
+
+
+def test_adjoint_sensitivity_matches_finite_differences():
+    p = HS.Params(2, 24, 16)
+    s = np.clip(HS.grf_design(2, 24, 16, seed=1, sigma=3.0), 0.05, 0.95)
+    hs = HeatSinkDesign(p, "fp64")
+    r0 = hs.iterate(s, tol=1e-10, max_steps=400000, filtered=s)
+    assert r0["forward"][0] == 1 and r0["adjoint"][0] == 1   # both converged
+    eps, ratios = 1e-4, []
+    for (i, j) in [(2, 1), (10, 5), (18, 12), (5, 8)]:
+        idx = i + p.lx * j
+        sp, sm = s.copy(), s.copy()
+        sp[idx] += eps
+        sm[idx] -= eps
+        fp = hs.iterate(s, tol=1e-10, max_steps=400000, filtered=sp)["objective"]
+        fm = hs.iterate(s, tol=1e-10, max_steps=400000, filtered=sm)["objective"]
+        fd = (fp - fm) / (2 * eps)
+        assert abs(fd) > 0
+        ratios.append(r0["dfdss"][idx] / fd)
+    hs.close()
+    ratios = np.array(ratios)
+    assert np.all(ratios > 0)
+    assert np.max(np.abs(ratios / ratios.mean() - 1.0)) < 0.02, ratios

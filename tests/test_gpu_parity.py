@@ -454,3 +454,23 @@ def test_graph_steps_equal_eager_steps(o, q, n):
         out.append((lp.get_populations(0), lp.get_populations(1)))
         lp.close()
     assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+
+
+@pytest.mark.parametrize("q", [9, 15])
+@pytest.mark.parametrize("storage", ["fp16", "bf16"])
+def test_heatsink_forward_16bit_storage(o, q, storage):
+    """Shifted 16-bit population storage (f - w_c * shift, FP32 compute) against the FP64 oracle
+    after 60 heat-sink steps. Tolerance, relative to max(1, max |field|): 5e-4 for FP16, 5e-3 for
+    BF16 (measured on GB300: FP16 g / T within 3e-4 / 2e-4 of their maxima, BF16 within
+    2.2e-3 / 2.7e-3)."""
+    rng = np.random.default_rng(5)
+    p = _heatsink_case(q)
+    lp, (f, g, mac, snap), _, _, _, _ = _run_forward(o, p, storage, 60, rng)
+    tol = 5e-4 if storage == "fp16" else 5e-3
+    close64(lp.get_populations(0), f, tol)
+    close64(lp.get_populations(1), g, tol)
+    for m, nm in enumerate(FWD_NAMES):
+        if q == 9 and nm.endswith("z"):
+            continue
+        close64(lp.get_field(A.RHO + m), mac[nm], tol)
+    lp.close()
