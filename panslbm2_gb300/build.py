@@ -2,7 +2,8 @@
 
 Translation units compile in parallel. The FP64 instantiation units are compiled with
 -fmad=false so their arithmetic matches the reference's scalar CPU path operation for
-operation; every other unit keeps FMA contraction (the throughput path).
+operation; every other unit keeps FMA contraction (the throughput path), and the FP32 / 16-bit
+instantiation units use the fast single-precision division (-prec-div=false, within 2 ulp).
 """
 import concurrent.futures as cf
 import os
@@ -44,6 +45,8 @@ def _compile(src, verbose_ptxas=False):
     flags = list(COMMON)
     if "_f64" in os.path.basename(src):
         flags += ["-fmad=false"]
+    elif "inst_" in os.path.basename(src):
+        flags += ["-prec-div=false"]
     if verbose_ptxas:
         flags += ["-Xptxas", "-v"]
     cmd = [nvcc()] + ARCH + flags + ["-c", src, "-o", obj]
