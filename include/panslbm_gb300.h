@@ -225,6 +225,24 @@ int pl_density_filter(pl_lattice h, double R, const double *v, const int *mask, 
 /* Normalize (normalize.h:8-23), in place on a host array of n */
 int pl_normalize(pl_lattice h, double *v, int n);
 
+/* MMA design-variable update on the device (Svanberg's method of moving asymptotes), FP64:
+ * replaces MMA<T>(n, m, a0, a, c, d, xmin, xmax) (utility/mma.h:62-86) and
+ * MMA<T>::UpdateVariables (utility/mma.h:196-548) for 1 <= m <= 4 constraints. Host arrays:
+ * a, c, d of m; xmin, xmax, xk, dfdx of n; g of m; dgdx of m rows of n. xk is updated in place.
+ * pl_mma_set_param: which 0 move, 1 asyinit, 2 asydecr, 3 asyincr, 4 albefa, 5 raa0, 6 epsvalue
+ * (the public members of MMA<T>, mma.h:97-105; defaults 0.5, 0.5, 0.7, 1.2, 0.1, 1e-5, 1e-6). */
+typedef struct pl_mma_s *pl_mma;
+int pl_mma_create(int n, int m, double a0, const double *a, const double *c, const double *d, const double *xmin,
+                  const double *xmax, pl_mma *out);
+int pl_mma_set_param(pl_mma h, int which, double value);
+int pl_mma_update(pl_mma h, double *xk, double f, const double *dfdx, const double *g, const double *dgdx);
+int pl_mma_destroy(pl_mma h);
+/* the optimizer's history, for ImportSetting / ExportSetting (mma.h:142-194): outer counter k,
+ * previous objective, x of the two previous updates, asymptotes L and U (host arrays of n) */
+int pl_mma_get_state(pl_mma h, int *k, double *previous, double *xkm2, double *xkm1, double *L, double *U);
+int pl_mma_set_state(pl_mma h, int k, double previous, const double *xkm2, const double *xkm1, const double *L,
+                     const double *U);
+
 /* last step kernel time (ms) measured with CUDA events on the lattice stream, and number
  * of kernels launched since creation */
 int pl_stats(pl_lattice h, double *last_step_ms, long long *launches);

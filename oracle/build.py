@@ -59,6 +59,21 @@ def build_ref(force=False):
     return out
 
 
+def build_ref_mma(force=False):
+    """The reference's own MMA<double> behind a C entry point (golden vectors of the MMA update);
+    None when the reference sources are absent."""
+    root = reference_root()
+    if root is None:
+        return None
+    outdir = os.path.join(HERE, "_ref")
+    os.makedirs(outdir, exist_ok=True)
+    out = os.path.join(outdir, "libref_mma.so")
+    src = os.path.join(HERE, "ref_mma.cpp")
+    if force or not _newer(out, [src]):
+        subprocess.check_call(["g++", "-std=c++17", "-I", root, "-w"] + FLAGS + ["-o", out, src])
+    return out
+
+
 if __name__ == "__main__":
     print(build_oracle(force="-f" in sys.argv))
     print(build_ref(force="-f" in sys.argv))

@@ -52,7 +52,8 @@ EXPORTS = [
     "pl_program_create", "pl_program_destroy", "pl_init", "pl_collide", "pl_step", "pl_steps", "pl_stream",
     "pl_solve", "pl_snapshot", "pl_set_snapshot", "pl_residual", "pl_residual_host", "pl_residual_device_noalloc",
     "pl_sensitivity", "pl_heaviside_var",
-    "pl_heaviside_sens", "pl_density_filter", "pl_normalize", "pl_stats",
+    "pl_heaviside_sens", "pl_density_filter", "pl_normalize", "pl_stats", "pl_mma_create", "pl_mma_set_param",
+    "pl_mma_update", "pl_mma_destroy", "pl_mma_get_state", "pl_mma_set_state",
 ]
 
 _lib = None

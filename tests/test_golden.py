@@ -12,7 +12,7 @@ from oracle import build as obuild
 from tests.golden import cases as C
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-FILES = sorted(glob.glob(os.path.join(HERE, "golden", "*.npz")))
+FILES = sorted(f for f in glob.glob(os.path.join(HERE, "golden", "*.npz")) if not os.path.basename(f).startswith("mma_"))
 
 
 @pytest.fixture(scope="module")
@@ -36,6 +36,15 @@ def test_oracle_matches_reference_golden(oracle, path):
     for k in out:
         assert np.array_equal(got[k], out[k]), "%s: %s differs, max abs %.3e" % (
             name, k, float(np.max(np.abs(got[k] - out[k]))) if out[k].size else 0.0)
+
+
+@pytest.mark.skipif(obuild.reference_root() is None, reason="reference sources not present")
+def test_mma_fixtures_are_the_reference_output():
+    """The MMA fixtures (tests/golden/mma_*.npz) are what the reference's MMA<double> produces."""
+    from tests.golden import make_golden as MG
+    for name in MG.MMA_CASES:
+        inp, out = C.load(os.path.join(HERE, "golden", name + ".npz"))
+        assert np.array_equal(MG.mma_reference(inp)["xhist"], out["xhist"]), name
 
 
 def test_fixture_inputs_regenerate(oracle):
