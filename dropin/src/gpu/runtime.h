@@ -466,7 +466,8 @@ struct Pair {
     template <class T>
     void collide(int kind, const pl_phys &ph, bool save, T *const *outs, int nouts, T *snap) {
         const bool adjoint = kind >= PL_ANS_BRINKMAN;
-        const bool has_g = !(kind == PL_NS_COLLIDE || kind == PL_NS_BRINKMAN || kind == PL_ANS_BRINKMAN);
+        const bool has_g = !(kind == PL_NS_COLLIDE || kind == PL_NS_BRINKMAN || kind == PL_ANS_BRINKMAN ||
+                             kind == PL_NSIN_COLLIDE || kind == PL_NSIN_BRINKMAN || kind == PL_ANSIN_BRINKMAN);
         const int slot = adjoint ? 1 : 0;
         const bool saves_snap = save && snap != nullptr;
         std::vector<int> idx;

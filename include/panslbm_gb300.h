@@ -47,11 +47,14 @@ extern "C" {
 #define PL_AD_HEATEX 4            /* AD::MacroBrinkmanCollideHeatExchange     advection.h:714-810      */
 #define PL_AD_NATURAL_NOBRINK 5   /* AD::MacroCollideNaturalConvection        advection.h:616-712      */
 #define PL_AD_FORCE_NOBRINK 6     /* AD::MacroCollideForceConvection          advection.h:528-614      */
+#define PL_NSIN_COLLIDE 7         /* NSin::MacroCollide (D2Q9)                nsincompressible.h:144-169 */
+#define PL_NSIN_BRINKMAN 8        /* NSin::MacroBrinkmanCollide (D2Q9)        nsincompressible.h:171-200 */
 #define PL_ANS_BRINKMAN 10        /* ANS::MacroBrinkmanCollide                adjointnavierstokes.h:396-470 */
 #define PL_AAD_NATURAL 11         /* AAD::MacroBrinkmanCollideNaturalConvection adjointadvection.h:1111-1230 */
 #define PL_AAD_FORCE 12           /* AAD::MacroBrinkmanCollideForceConvection adjointadvection.h:995-1109 */
 #define PL_AAD_HEATEX 13          /* AAD::MacroBrinkmanCollideHeatExchange    adjointadvection.h:892-993 */
 #define PL_AAD_MASSFLOW 14        /* AAD::MacroBrinkmanCollideNaturalConvectionMassFlow adjointadvection.h:1232-1355 */
+#define PL_ANSIN_BRINKMAN 15      /* ANSin::MacroBrinkmanCollide (D2Q9)       adjointnsincompressible.h:143-178 */
 
 /* boundary-program op kinds */
 #define PL_BC_WALL 0      /* (D2Q9|D3Q15)::BoundaryConditionAlong*   type: 1 BARRIER, 2 MIRROR  */
@@ -66,6 +69,10 @@ extern "C" {
 #define PL_BC_AAD_T 9     /* AAD::iBoundaryConditionSetTAlong*                                   */
 #define PL_BC_AAD_Q 10    /* AAD::iBoundaryConditionSetQAlong*      `eps`                        */
 #define PL_BC_AAD_RHO 11  /* AAD::iBoundaryConditionSetRhoAlong*    type: 1 SetT, 2 SetQ; `eps`  */
+#define PL_BC_NSIN_U 12   /* NSin::BoundaryConditionSetUAlong{X,Y}Edge   v0,v1 = ux,uy (D2Q9)    */
+#define PL_BC_NSIN_RHO 13 /* NSin::BoundaryConditionSetRhoAlong{X,Y}Edge v0 = rho, v1 = us      */
+#define PL_BC_ANSIN_U 14  /* ANSin::iBoundaryConditionSetUAlong{X,Y}Edge `eps`; ANSin's iSetRho
+                           * is ANS's (PL_BC_ANS_RHO)                                            */
 #define PL_SMOOTH_CORNER 20  /* SmoothCorner()                                                   */
 #define PL_SMOOTH_AT 21      /* SmoothCornerAt(i,j[,k],di,dj[,dk])                               */
 #define PL_SMOOTH_LINE 22    /* SmoothCornerAlong{YZ,ZX,XY}: axis = 0,1,2; (i,j) = line, (di,dj)  */
@@ -162,7 +169,8 @@ int pl_program_create(pl_lattice h, const pl_bc_desc *descs, int n, int *prog);
 int pl_program_destroy(pl_lattice h, int prog);
 
 /* initial conditions: which 0 NS::InitialCondition(rho,u), 1 AD::(T,u), 2 ANS::(u; ip,iu),
- * 3 AAD::(u; iT,iq). a0..a3 = the scalar/vector inputs, ux..uz = the velocity argument. */
+ * 3 AAD::(u; iT,iq), 4 NSin::(rho,u), 5 ANSin::(ip,iu) (D2Q9; ux, uy may be NULL).
+ * a0..a3 = the scalar/vector inputs, ux..uz = the velocity argument. */
 int pl_init(pl_lattice h, int which, const double *a0, const double *a1, const double *a2, const double *a3,
             const double *ux, const double *uy, const double *uz);
 

@@ -16,10 +16,12 @@ IP = C.POINTER(C.c_int)
 
 # collide kinds
 NS_COLLIDE, NS_BRINKMAN, AD_NATURAL, AD_FORCE, AD_HEATEX, AD_NATURAL_NOBRINK, AD_FORCE_NOBRINK = 0, 1, 2, 3, 4, 5, 6
-ANS_BRINKMAN, AAD_NATURAL, AAD_FORCE, AAD_HEATEX, AAD_MASSFLOW = 10, 11, 12, 13, 14
+NSIN_COLLIDE, NSIN_BRINKMAN = 7, 8
+ANS_BRINKMAN, AAD_NATURAL, AAD_FORCE, AAD_HEATEX, AAD_MASSFLOW, ANSIN_BRINKMAN = 10, 11, 12, 13, 14, 15
 # bc kinds
 BC_WALL, BC_IWALL, BC_NS_U, BC_NS_RHO, BC_AD_T, BC_AD_Q, BC_AD_QC = 0, 1, 2, 3, 4, 5, 6
 BC_ANS_U, BC_ANS_RHO, BC_AAD_T, BC_AAD_Q, BC_AAD_RHO = 7, 8, 9, 10, 11
+BC_NSIN_U, BC_NSIN_RHO, BC_ANSIN_U = 12, 13, 14
 
 
 class Lat(C.Structure):

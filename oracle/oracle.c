@@ -335,6 +335,59 @@ static void ans_node(const lat_t *t, int idx, int i, int j, int k, void *vctx) {
     (void)i; (void)j; (void)k;
 }
 
+/* ---- incompressible NS boundary conditions (D2Q9) -------------------------------------
+ * NSin::BoundaryConditionSetUAlong{X,Y}Edge (nsincompressible.h:46-90) and SetRhoAlong*
+ * (92-140). With the edge normal a, tangent b and side d: the unknown normal population is its
+ * opposite - d (2 u_n / 3); an unknown diagonal is its opposite - d (u_n / 6) - c_b (f_b+ - f_b- - u_t) / 2.
+ * SetRho first recovers u_n = -d (rho - S), S = f_0 + f_b+ + f_b- + 2 (sum of the known normal
+ * and diagonal populations of side d, increasing c).
+ * ANSin::iBoundaryConditionSetUAlong{X,Y}Edge (adjointnsincompressible.h:49-92): every unknown
+ * adjoint population is its opposite - 2 eps / 3. */
+static int straight2(const lat_t *t, int a, int s) {
+    for (int c = 1; c < t->q; ++c) if (t->c[a][c] == s && t->c[1 - a][c] == 0) return c;
+    return 0;
+}
+static void nsin_node(const lat_t *t, int idx, int i, int j, int k, void *vctx) {
+    bcctx *x = (bcctx *)vctx;
+    const ol_bc *bc = x->bc;
+    if (!bc->type[idx]) return;
+    double *f = x->f;
+    int a = bc->axis, d = bc->dir, b = 1 - a;
+    if (bc->kind == OL_BC_ANSIN_U) {
+        for (int c = 1; c < t->q; ++c)
+            if (t->c[a][c] == d) F(f, c, idx) = F(f, opp_of(t, c), idx) - 2.0 * bc->eps / 3.0;
+        return;
+    }
+    int tp = straight2(t, b, 1), tm = straight2(t, b, -1);
+    double un, ut;
+    if (bc->kind == OL_BC_NSIN_U) {
+        un = (a == 0) ? bc->v0[idx] : bc->v1[idx];
+        ut = (a == 0) ? bc->v1[idx] : bc->v0[idx];
+    } else {
+        double rho = bc->v0[idx], so = 0.0;
+        int first = 1;
+        ut = bc->v1[idx];
+        for (int c = 1; c < t->q; ++c) {
+            if (t->c[a][c] != d) continue;
+            if (first) { so = F(f, c, idx); first = 0; } else so += F(f, c, idx);
+        }
+        double S = F(f, 0, idx) + F(f, tp, idx) + F(f, tm, idx) + 2.0 * so;
+        un = (d < 0) ? rho - S : -rho + S;
+    }
+    double X = F(f, tp, idx) - F(f, tm, idx) - ut;
+    for (int c = 1; c < t->q; ++c) {
+        if (t->c[a][c] != -d) continue;
+        double v = F(f, opp_of(t, c), idx);
+        if (t->c[b][c] == 0) {
+            F(f, c, idx) = (d < 0) ? v + 2.0 * un / 3.0 : v - 2.0 * un / 3.0;
+        } else {
+            v = (d < 0) ? v + un / 6.0 : v - un / 6.0;
+            F(f, c, idx) = (t->c[b][c] > 0) ? v - 0.5 * X : v + 0.5 * X;
+        }
+    }
+    (void)i; (void)j; (void)k;
+}
+
 /* ---- AAD adjoint BCs ------------------------------------------------------------------
  * AAD::iBoundaryConditionSetTAlong* (adjointadvection.h:152-300), iSetQAlong* (302-484,
  * with the missing 3.0 factors on the +y / +-z D3Q15 faces kept), iSetRhoAlong* (486-751). */
@@ -435,6 +488,7 @@ void ol_apply_bc(const ol_lat *L, double *f, double *g, const ol_bc *bc) {
     case OL_BC_AD_T: case OL_BC_AD_Q: case OL_BC_AD_QC: fn = adbc_node; break;
     case OL_BC_ANS_U: case OL_BC_ANS_RHO: fn = ans_node; break;
     case OL_BC_AAD_T: case OL_BC_AAD_Q: case OL_BC_AAD_RHO: fn = aad_node; break;
+    case OL_BC_NSIN_U: case OL_BC_NSIN_RHO: case OL_BC_ANSIN_U: if (t->nd != 2) return; fn = nsin_node; break;
     default: return;
     }
     for_face(t, bc->axis, bc->pos, fn, &x);
@@ -672,13 +726,61 @@ static inline void bgk(const lat_t *t, double *f, const double *feq, double om) 
     for (int c = 0; c < t->q; ++c) f[c] = iom * f[c] + om * feq[c];
 }
 
+/* ---- incompressible variants (D2Q9 only in the reference) ------------------------------ */
+/* NSin::Macro (nsincompressible.h:13-25): rho and the momentum sums, no division by rho */
+static void nsin_macro(const lat_t *t, const double *f, double *rho, double *u) {
+    double r = f[0], m[2] = {0.0, 0.0};
+    for (int c = 1; c < t->q; ++c) {
+        double v = f[c];
+        r += v;
+        for (int b = 0; b < 2; ++b) m[b] += t->c[b][c] * v;
+    }
+    *rho = r;
+    u[0] = m[0]; u[1] = m[1]; u[2] = 0.0;
+}
+/* NSin::Equilibrium (nsincompressible.h:27-35): w (3 c.u + 4.5 (c.u)^2 + rho - 1.5 u.u) */
+static void nsin_eq(const lat_t *t, double *feq, double rho, const double *u) {
+    double rhouu = rho - 1.5 * (u[0] * u[0] + u[1] * u[1]);
+    for (int c = 0; c < t->q; ++c) {
+        double ciu = t->c[0][c] * u[0] + t->c[1][c] * u[1];
+        feq[c] = t->w[c] * (3.0 * ciu + 4.5 * ciu * ciu + rhouu);
+    }
+}
+/* NSin::ExternalForceBrinkman (nsincompressible.h:37-44) has NS's form: ns_brinkman. */
+/* ANSin::Macro (adjointnsincompressible.h:13-30): ip = sum w f, iu_b = sum w f (c_b + 3 (c.u) c_b - u_b),
+ * im_b = sum w f c_b */
+static void ansin_macro(const lat_t *t, const double *f, const double *u, double *ip, double *iu, double *im) {
+    double w0 = t->w[0];
+    *ip = f[0] * w0;
+    for (int b = 0; b < 2; ++b) { iu[b] = -f[0] * w0 * u[b]; im[b] = 0.0; }
+    for (int c = 1; c < t->q; ++c) {
+        double ciu = t->c[0][c] * u[0] + t->c[1][c] * u[1];
+        double fei = f[c] * t->w[c];
+        *ip += fei;
+        for (int b = 0; b < 2; ++b) iu[b] += fei * (t->c[b][c] + 3.0 * ciu * t->c[b][c] - u[b]);
+        for (int b = 0; b < 2; ++b) im[b] += fei * t->c[b][c];
+    }
+    iu[2] = 0.0; im[2] = 0.0;
+}
+/* ANSin::Equilibrium (adjointnsincompressible.h:32-38): ip + 3 iu.c */
+static void ansin_eq(const lat_t *t, double *feq, double ip, const double *iu) {
+    for (int c = 0; c < t->q; ++c) feq[c] = ip + 3.0 * (iu[0] * t->c[0][c] + iu[1] * t->c[1][c]);
+}
+/* ANSin::ExternalForceBrinkman (adjointnsincompressible.h:40-47): f_c -= 3 alpha/(1 + alpha) c.im */
+static void ansin_brinkman(const lat_t *t, double *f, const double *im, double alpha) {
+    double coef = 3.0 * alpha / (1.0 + alpha);
+    for (int c = 1; c < t->q; ++c) f[c] -= coef * (t->c[0][c] * im[0] + t->c[1][c] * im[1]);
+}
+
 /* ---- collide kernels ------------------------------------------------------------------
  * NS::MacroCollide / MacroBrinkmanCollide (navierstokes.h:430-546)
  * AD::MacroCollide{Force,Natural}Convection (advection.h:528-712),
  *     MacroBrinkmanCollide{HeatExchange,ForceConvection,NaturalConvection} (714-1044)
  * ANS::MacroBrinkmanCollide (adjointnavierstokes.h:396-470)
  * AAD::MacroBrinkmanCollide{HeatExchange,ForceConvection,NaturalConvection,
- *     NaturalConvectionMassFlow} (adjointadvection.h:892-1355) */
+ *     NaturalConvectionMassFlow} (adjointadvection.h:892-1355)
+ * NSin::MacroCollide / MacroBrinkmanCollide (nsincompressible.h:144-200),
+ * ANSin::MacroBrinkmanCollide (adjointnsincompressible.h:143-178) */
 void ol_collide(const ol_lat *L, int kind, double *fa, double *ga, const ol_fields *Fd, const ol_phys *P, int save) {
     lat_t T = mk(L); const lat_t *t = &T;
     const int n = t->n, q = t->q, nd = t->nd;
@@ -695,7 +797,29 @@ void ol_collide(const ol_lat *L, int kind, double *fa, double *ga, const ol_fiel
             omg = 1.0 / (3.0 * Fd->diffusivity[idx] + 0.5);
         else if (ga)
             omg = 1.0 / (3.0 * P->diff + 0.5);
-        if (kind <= OL_AD_FORCE_NOBRINK) {
+        if (kind == OL_NSIN_COLLIDE || kind == OL_NSIN_BRINKMAN) {
+            double rho, u[3];
+            nsin_macro(t, f, &rho, u);
+            if (kind == OL_NSIN_BRINKMAN) {
+                ns_brinkman(t, f, rho, u, Fd->alpha[idx]);
+                nsin_macro(t, f, &rho, u);
+            }
+            if (save) { Fd->rho[idx] = rho; Fd->ux[idx] = u[0]; Fd->uy[idx] = u[1]; }
+            nsin_eq(t, feq, rho, u);
+            bgk(t, f, feq, omf);
+        } else if (kind == OL_ANSIN_BRINKMAN) {
+            double u[3] = {Fd->ux[idx], Fd->uy[idx], 0.0};
+            double ip, iu[3], im[3];
+            ansin_macro(t, f, u, &ip, iu, im);
+            ansin_brinkman(t, f, im, Fd->alpha[idx]);
+            ansin_macro(t, f, u, &ip, iu, im);
+            if (save) {
+                Fd->ip[idx] = ip; Fd->iux[idx] = iu[0]; Fd->iuy[idx] = iu[1];
+                Fd->imx[idx] = im[0]; Fd->imy[idx] = im[1];
+            }
+            ansin_eq(t, feq, ip, iu);
+            bgk(t, f, feq, omf);
+        } else if (kind <= OL_AD_FORCE_NOBRINK) {
             double rho, u[3], tem = 0.0, qv[3] = {0, 0, 0};
             ns_macro(t, f, &rho, u);
             if (ga) ad_macro(t, g, u, omg, &tem, qv);
@@ -771,7 +895,8 @@ void ol_collide(const ol_lat *L, int kind, double *fa, double *ga, const ol_fiel
 }
 
 /* ---- initial conditions: NS::InitialCondition (navierstokes.h:548-572), AD:: (advection.h:
- *      1046-1070), ANS:: (adjointnavierstokes.h:472-498), AAD:: (adjointadvection.h:1357-1381) */
+ *      1046-1070), ANS:: (adjointnavierstokes.h:472-498), AAD:: (adjointadvection.h:1357-1381),
+ *      NSin:: (nsincompressible.h:202-212), ANSin:: (adjointnsincompressible.h:180-192) */
 void ol_init(const ol_lat *L, int which, double *fa, const ol_fields *Fd) {
     lat_t T = mk(L); const lat_t *t = &T;
     const int n = t->n, q = t->q, nd = t->nd;
@@ -784,6 +909,11 @@ void ol_init(const ol_lat *L, int which, double *fa, const ol_fields *Fd) {
         else if (which == 2) {
             double iu[3] = {Fd->iux[idx], Fd->iuy[idx], nd == 3 ? Fd->iuz[idx] : 0.0};
             ans_eq(t, eq, u, Fd->ip[idx], iu);
+        } else if (which == 4) {
+            nsin_eq(t, eq, Fd->rho[idx], u);
+        } else if (which == 5) {
+            double iu[3] = {Fd->iux[idx], Fd->iuy[idx], 0.0};
+            ansin_eq(t, eq, Fd->ip[idx], iu);
         } else {
             double iq[3] = {Fd->iqx[idx], Fd->iqy[idx], nd == 3 ? Fd->iqz[idx] : 0.0};
             aad_eq(t, eq, Fd->item[idx], iq, u);

@@ -55,11 +55,14 @@ enum {
     OL_AD_HEATEX = 4,             /* AD::MacroBrinkmanCollideHeatExchange                */
     OL_AD_NATURAL_NOBRINK = 5,    /* AD::MacroCollideNaturalConvection                   */
     OL_AD_FORCE_NOBRINK = 6,      /* AD::MacroCollideForceConvection                     */
+    OL_NSIN_COLLIDE = 7,          /* NSin::MacroCollide (D2Q9)                           */
+    OL_NSIN_BRINKMAN = 8,         /* NSin::MacroBrinkmanCollide (D2Q9)                   */
     OL_ANS_BRINKMAN = 10,         /* ANS::MacroBrinkmanCollide                           */
     OL_AAD_NATURAL = 11,          /* AAD::MacroBrinkmanCollideNaturalConvection          */
     OL_AAD_FORCE = 12,            /* AAD::MacroBrinkmanCollideForceConvection            */
     OL_AAD_HEATEX = 13,           /* AAD::MacroBrinkmanCollideHeatExchange               */
-    OL_AAD_MASSFLOW = 14          /* AAD::MacroBrinkmanCollideNaturalConvectionMassFlow  */
+    OL_AAD_MASSFLOW = 14,         /* AAD::MacroBrinkmanCollideNaturalConvectionMassFlow  */
+    OL_ANSIN_BRINKMAN = 15        /* ANSin::MacroBrinkmanCollide (D2Q9)                  */
 };
 
 /* Boundary-condition kinds applied along one edge (2D) / face (3D) */
@@ -75,7 +78,11 @@ enum {
     OL_BC_ANS_RHO = 8,    /* ANS::iBoundaryConditionSetRhoAlong*                             */
     OL_BC_AAD_T = 9,      /* AAD::iBoundaryConditionSetTAlong*                               */
     OL_BC_AAD_Q = 10,     /* AAD::iBoundaryConditionSetQAlong*   (eps)                       */
-    OL_BC_AAD_RHO = 11    /* AAD::iBoundaryConditionSetRhoAlong* (type[]: 1 SetT, 2 SetQ; eps; acts on f and g) */
+    OL_BC_AAD_RHO = 11,   /* AAD::iBoundaryConditionSetRhoAlong* (type[]: 1 SetT, 2 SetQ; eps; acts on f and g) */
+    OL_BC_NSIN_U = 12,    /* NSin::BoundaryConditionSetUAlong{X,Y}Edge   (v0,v1 = ux,uy)     */
+    OL_BC_NSIN_RHO = 13,  /* NSin::BoundaryConditionSetRhoAlong{X,Y}Edge (v0 = rho, v1 = us) */
+    OL_BC_ANSIN_U = 14    /* ANSin::iBoundaryConditionSetUAlong{X,Y}Edge (eps); ANSin's iSetRho
+                           * is ANS's (OL_BC_ANS_RHO)                                      */
 };
 
 typedef struct {
@@ -111,7 +118,7 @@ void ol_smooth_line(const ol_lat *L, double *f, int plane, int a, int b, int da,
 void ol_collide(const ol_lat *L, int kind, double *f, double *g, const ol_fields *F,
                 const ol_phys *P, int save);
 
-/* Initial conditions: 0 NS, 1 AD, 2 ANS, 3 AAD */
+/* Initial conditions: 0 NS, 1 AD, 2 ANS, 3 AAD, 4 NSin (rho, u), 5 ANSin (ip, iu) */
 void ol_init(const ol_lat *L, int which, double *f, const ol_fields *F);
 
 /* Sensitivities.

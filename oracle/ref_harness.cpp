@@ -22,6 +22,10 @@
 #include "src/equation/advection.h"
 #include "src/equation/adjointnavierstokes.h"
 #include "src/equation/adjointadvection.h"
+#if REF_DIM == 2
+#include "src/equation/nsincompressible.h"
+#include "src/equation/adjointnsincompressible.h"
+#endif
 #include "src/utility/heavisidefilter.h"
 #include "src/utility/densityfilter.h"
 #include "src/utility/residual.h"
@@ -96,6 +100,9 @@ extern "C" void NAME(apply_bc)(const ol_lat *L, double *f, double *g, const ol_b
     case OL_BC_AAD_T: if (a == 0) AAD::iBoundaryConditionSetTAlongXEdge(*p, pos, d, bc->ux, bc->uy, T); else AAD::iBoundaryConditionSetTAlongYEdge(*p, pos, d, bc->ux, bc->uy, T); break;
     case OL_BC_AAD_Q: if (a == 0) AAD::iBoundaryConditionSetQAlongXEdge(*p, pos, d, bc->ux, bc->uy, T, bc->eps); else AAD::iBoundaryConditionSetQAlongYEdge(*p, pos, d, bc->ux, bc->uy, T, bc->eps); break;
     case OL_BC_AAD_RHO: if (a == 0) AAD::iBoundaryConditionSetRhoAlongXEdge(*p, *q, pos, d, bc->rho, bc->ux, bc->uy, bc->tem, T, bc->eps); else AAD::iBoundaryConditionSetRhoAlongYEdge(*p, *q, pos, d, bc->rho, bc->ux, bc->uy, bc->tem, T, bc->eps); break;
+    case OL_BC_NSIN_U: if (a == 0) NSin::BoundaryConditionSetUAlongXEdge(*p, pos, d, V0, V1, T); else NSin::BoundaryConditionSetUAlongYEdge(*p, pos, d, V0, V1, T); break;
+    case OL_BC_NSIN_RHO: if (a == 0) NSin::BoundaryConditionSetRhoAlongXEdge(*p, pos, d, V0, V1, T); else NSin::BoundaryConditionSetRhoAlongYEdge(*p, pos, d, V0, V1, T); break;
+    case OL_BC_ANSIN_U: if (a == 0) ANSin::iBoundaryConditionSetUAlongXEdge(*p, pos, d, T, bc->eps); else ANSin::iBoundaryConditionSetUAlongYEdge(*p, pos, d, T, bc->eps); break;
     }
 #else
     auto T = FI(ty[NID(i, j, k)]);
@@ -168,6 +175,9 @@ extern "C" void NAME(collide)(const ol_lat *L, int kind, double *f, double *g, c
     case OL_AAD_FORCE: AAD::MacroBrinkmanCollideForceConvection(*p, F->rho, F->ux, F->uy, F->ip, F->iux, F->iuy, F->imx, F->imy, F->alpha, nu, *q, F->tem, F->item, F->iqx, F->iqy, F->diffusivity, save, F->gsnap); break;
     case OL_AAD_HEATEX: AAD::MacroBrinkmanCollideHeatExchange(*p, F->rho, F->ux, F->uy, F->ip, F->iux, F->iuy, F->imx, F->imy, F->alpha, nu, *q, F->tem, F->item, F->iqx, F->iqy, F->beta, diff, save); break;
     case OL_AAD_MASSFLOW: AAD::MacroBrinkmanCollideNaturalConvectionMassFlow(*p, F->rho, F->ux, F->uy, F->ip, F->iux, F->iuy, F->imx, F->imy, F->alpha, nu, *q, F->tem, F->item, F->iqx, F->iqy, F->diffusivity, gx, gy, F->dirx, F->diry, save, F->gsnap); break;
+    case OL_NSIN_COLLIDE: NSin::MacroCollide(*p, F->rho, F->ux, F->uy, nu, save); break;
+    case OL_NSIN_BRINKMAN: NSin::MacroBrinkmanCollide(*p, F->rho, F->ux, F->uy, nu, F->alpha, save); break;
+    case OL_ANSIN_BRINKMAN: ANSin::MacroBrinkmanCollide(*p, F->rho, F->ux, F->uy, F->ip, F->iux, F->iuy, F->imx, F->imy, nu, F->alpha, save); break;
     }
 #else
     double gz = P->gz;
@@ -198,6 +208,8 @@ extern "C" void NAME(init)(const ol_lat *L, int which, double *f, const ol_field
     if (which == 0) NS::InitialCondition(*p, F->rho, F->ux, F->uy);
     else if (which == 1) AD::InitialCondition(*p, F->tem, F->ux, F->uy);
     else if (which == 2) ANS::InitialCondition(*p, F->ux, F->uy, F->ip, F->iux, F->iuy);
+    else if (which == 4) NSin::InitialCondition(*p, F->rho, F->ux, F->uy);
+    else if (which == 5) ANSin::InitialCondition(*p, F->ux, F->uy, F->ip, F->iux, F->iuy);
     else AAD::InitialCondition(*p, F->ux, F->uy, F->item, F->iqx, F->iqy);
 #else
     if (which == 0) NS::InitialCondition(*p, F->rho, F->ux, F->uy, F->uz);

@@ -17,10 +17,12 @@ STORAGE = {"fp64": PL_FP64, "fp32": PL_FP32, "fp16": PL_FP16, "bf16": PL_BF16}
 
 # collide kinds
 NS_COLLIDE, NS_BRINKMAN, AD_NATURAL, AD_FORCE, AD_HEATEX, AD_NATURAL_NOBRINK, AD_FORCE_NOBRINK = 0, 1, 2, 3, 4, 5, 6
-ANS_BRINKMAN, AAD_NATURAL, AAD_FORCE, AAD_HEATEX, AAD_MASSFLOW = 10, 11, 12, 13, 14
+NSIN_COLLIDE, NSIN_BRINKMAN = 7, 8
+ANS_BRINKMAN, AAD_NATURAL, AAD_FORCE, AAD_HEATEX, AAD_MASSFLOW, ANSIN_BRINKMAN = 10, 11, 12, 13, 14, 15
 # boundary op kinds
 BC_WALL, BC_IWALL, BC_NS_U, BC_NS_RHO, BC_AD_T, BC_AD_Q, BC_AD_QC = 0, 1, 2, 3, 4, 5, 6
 BC_ANS_U, BC_ANS_RHO, BC_AAD_T, BC_AAD_Q, BC_AAD_RHO = 7, 8, 9, 10, 11
+BC_NSIN_U, BC_NSIN_RHO, BC_ANSIN_U = 12, 13, 14
 SMOOTH_CORNER, SMOOTH_AT, SMOOTH_LINE = 20, 21, 22
 # fields
 ALPHA, KAPPA, BETA, DIRX, DIRY, DIRZ = 0, 1, 2, 3, 4, 5

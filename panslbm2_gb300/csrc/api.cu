@@ -153,7 +153,13 @@ int check_launch(pl_lattice h, int nk) {
     h->launches += nk;
     return PL_OK;
 }
-bool valid_kind(int k) { return (k >= 0 && k <= 6) || (k >= 10 && k <= 14); }
+bool valid_kind(int k) { return (k >= 0 && k <= 8) || (k >= 10 && k <= 15); }
+// NSin / ANSin exist for D2Q9 only (nsincompressible.h, adjointnsincompressible.h)
+int check_kind(pl_lattice h, int kind) {
+    if (!valid_kind(kind)) return fail(PL_ERR_ARG, "unknown collide kind %d", kind);
+    if (pl::kind_incompressible(kind) && h->nd != 2) return fail(PL_ERR_UNSUPPORTED, "kind %d is D2Q9 only", kind);
+    return PL_OK;
+}
 int field_index_c(int f) {
     if (f >= PL_ALPHA && f <= PL_DIRZ) return f;
     if (f >= PL_FWD_RHO && f <= PL_FWD_TEM) return 6 + (f - PL_FWD_RHO);
@@ -254,8 +260,10 @@ int compile_program(pl_lattice h, const pl_bc_desc *descs, int ndesc, Program &P
         }
         if (d.kind == PL_SMOOTH_AT) { smooth_at(d.lat, d.i, d.j, d.k, d.di, d.dj, d.dk); ++seq; continue; }
         if (d.kind == PL_SMOOTH_LINE) { smooth_line(d.lat, d.axis, d.i, d.j, d.di, d.dj); ++seq; continue; }
-        if (d.kind < PL_BC_WALL || d.kind > PL_BC_AAD_RHO)
+        if (d.kind < PL_BC_WALL || d.kind > PL_BC_ANSIN_U)
             return fail(PL_ERR_ARG, "program desc %d: unknown kind %d", di, d.kind);
+        if (d.kind >= PL_BC_NSIN_U && h->nd != 2)
+            return fail(PL_ERR_UNSUPPORTED, "program desc %d: kind %d is D2Q9 only", di, d.kind);
         if (d.axis < 0 || d.axis >= h->nd || (d.dir != -1 && d.dir != 1))
             return fail(PL_ERR_ARG, "program desc %d: axis %d / dir %d invalid", di, d.axis, d.dir);
         const int a = d.axis, p = d.pos;
@@ -533,7 +541,8 @@ int build_args(pl_lattice h, int kind, const pl_phys *ph, int prog, int src, int
     // inputs required by the kind
     int r;
     if (!kind_inputs) goto program;
-    if (kind == PL_NS_BRINKMAN || kind == PL_AD_NATURAL || kind == PL_AD_FORCE || kind == PL_AD_HEATEX || adjk) {
+    if (kind == PL_NS_BRINKMAN || kind == PL_NSIN_BRINKMAN || kind == PL_AD_NATURAL || kind == PL_AD_FORCE ||
+        kind == PL_AD_HEATEX || adjk) {
         if (!h->fld[PL_ALPHA]) return fail(PL_ERR_STATE, "kind %d needs PL_ALPHA", kind);
         if ((r = ensure_cfield(h, PL_ALPHA))) return r;
         a.alpha = h->cfld[0];
@@ -558,7 +567,8 @@ int build_args(pl_lattice h, int kind, const pl_phys *ph, int prog, int src, int
     if (adjk) {
         for (int f = PL_FWD_RHO; f <= PL_FWD_TEM; ++f) {
             if (f == PL_FWD_UZ && h->nd == 2) continue;
-            if (f == PL_FWD_TEM && kind == PL_ANS_BRINKMAN) continue;
+            if (f == PL_FWD_TEM && (kind == PL_ANS_BRINKMAN || kind == PL_ANSIN_BRINKMAN)) continue;
+            if (f == PL_FWD_RHO && kind == PL_ANSIN_BRINKMAN) continue;   // ANSin reads u only
             if (!h->fld[f]) return fail(PL_ERR_STATE, "adjoint kind %d needs the forward solution (pl_freeze_forward)", kind);
             if ((r = ensure_cfield(h, f))) return r;
             a.fwd[f - PL_FWD_RHO] = h->cfld[6 + f - PL_FWD_RHO];
@@ -631,7 +641,7 @@ void after_collide(pl_lattice h, int kind, bool save, int src, int prog, bool pu
 }
 
 int do_collide(pl_lattice h, int kind, const pl_phys *ph, bool save) {
-    if (!valid_kind(kind)) return fail(PL_ERR_ARG, "unknown collide kind %d", kind);
+    if (int e = check_kind(h, kind)) return e;
     const bool adjk = pl::kind_is_adjoint(kind);
     if (!adjk) save = true;   // boundary ops of the next step read this velocity
     KArgs a;
@@ -645,7 +655,7 @@ int do_collide(pl_lattice h, int kind, const pl_phys *ph, bool save) {
 }
 
 int do_step(pl_lattice h, int kind, const pl_phys *ph, int prog, bool save) {
-    if (!valid_kind(kind)) return fail(PL_ERR_ARG, "unknown collide kind %d", kind);
+    if (int e = check_kind(h, kind)) return e;
     const int bcu_slot = h->fwd_latest;
     KArgs a;
     int r = build_args(h, kind, ph, prog, h->cur, h->cur ^ 1, save, true, bcu_slot, a);
@@ -971,8 +981,11 @@ int pl_program_destroy(pl_lattice h, int prog) {
 
 int pl_init(pl_lattice h, int which, const double *a0, const double *a1, const double *a2, const double *a3,
             const double *ux, const double *uy, const double *uz) {
-    if (!h || which < 0 || which > 3 || !a0 || !ux || !uy || (h->nd == 3 && !uz)) return fail(PL_ERR_ARG, "bad arguments");
-    if (which >= 2 && (!a1 || !a2 || (h->nd == 3 && !a3))) return fail(PL_ERR_ARG, "adjoint init needs a1..a3");
+    if (!h || which < 0 || which > 5 || !a0) return fail(PL_ERR_ARG, "bad arguments");
+    if (which >= 4 && h->nd != 2) return fail(PL_ERR_UNSUPPORTED, "init %d is D2Q9 only", which);
+    if (which != 5 && (!ux || !uy || (h->nd == 3 && !uz))) return fail(PL_ERR_ARG, "init %d needs the velocity", which);
+    if ((which == 2 || which == 3 || which == 5) && (!a1 || !a2 || (h->nd == 3 && !a3)))
+        return fail(PL_ERR_ARG, "adjoint init needs a1..a3");
     double *buf;
     int r = scratch(h, 1, &buf);   // q*N doubles >= 7*N
     if (r) return r;

@@ -6,6 +6,8 @@
 //   AD           AD::BoundaryConditionSetT/SetQAlong* (advection.h:97-524)
 //   ANS adjoint  ANS::iBoundaryConditionSetU/SetRhoAlong* (adjointnavierstokes.h:95-392)
 //   AAD adjoint  AAD::iBoundaryConditionSetT/SetQ/SetRhoAlong* (adjointadvection.h:152-751)
+//   incompressible (D2Q9) NSin::BoundaryConditionSetU/SetRhoAlong* (nsincompressible.h:46-140),
+//                ANSin::iBoundaryConditionSetUAlong* (adjointnsincompressible.h:49-92)
 // The face of an op is (axis a, side d); "inward" populations have c_a == -d.
 #pragma once
 #include "physics.cuh"
@@ -305,6 +307,58 @@ __device__ __forceinline__ void apply_op(const Op &op, T *f, T *g, int node, con
         for (int c = 0; c < Q; ++c) src[c] = f[c];
 #pragma unroll
         for (int c = 1; c < Q; ++c) if (cmp<L>(c, A) == d) f[c] = src[opp_d<L>(c)] + r0 + flux0 + obj0;
+        break;
+    } break;
+    case BC_NSIN_U:
+    case BC_NSIN_RHO:
+    case BC_ANSIN_U: if constexpr (!SIMPLE && ND == 2) {
+        // NSin::BoundaryConditionSetU/SetRhoAlong{X,Y}Edge (nsincompressible.h:46-140),
+        // ANSin::iBoundaryConditionSetUAlong{X,Y}Edge (adjointnsincompressible.h:49-92)
+        T *p = f;
+        T src[Q];
+#pragma unroll
+        for (int c = 0; c < Q; ++c) src[c] = p[c];
+        if (op.kind == BC_ANSIN_U) {
+            const T de = T(2) * T(op.eps) / T(3);
+#pragma unroll
+            for (int c = 1; c < Q; ++c) if (cmp<L>(c, A) == d) p[c] = src[opp_d<L>(c)] - de;
+            break;
+        }
+        const int b = 1 - A;
+        T ftp = T(0), ftm = T(0);
+#pragma unroll
+        for (int c = 1; c < Q; ++c) {
+            if (cmp<L>(c, A) != 0) continue;
+            if (cmp<L>(c, b) == 1) ftp = src[c];
+            if (cmp<L>(c, b) == -1) ftm = src[c];
+        }
+        T un, ut;
+        if (op.kind == BC_NSIN_U) {
+            un = A == 0 ? T(op.v0) : T(op.v1);
+            ut = A == 0 ? T(op.v1) : T(op.v0);
+        } else {
+            const T rho = T(op.v0);
+            ut = T(op.v1);
+            T so = T(0);
+            bool first = true;
+#pragma unroll
+            for (int c = 1; c < Q; ++c)
+                if (cmp<L>(c, A) == d) { if (first) { so = src[c]; first = false; } else so += src[c]; }
+            const T S = src[0] + ftp + ftm + T(2) * so;
+            un = d < 0 ? rho - S : -rho + S;
+        }
+        const T X = ftp - ftm - ut;
+#pragma unroll
+        for (int c = 1; c < Q; ++c) {
+            if (cmp<L>(c, A) != -d) continue;
+            T v = src[opp_d<L>(c)];
+            if (cmp<L>(c, b) == 0) {
+                p[c] = d < 0 ? v + T(2) * un / T(3) : v - T(2) * un / T(3);
+            } else {
+                v = d < 0 ? v + un / T(6) : v - un / T(6);
+                p[c] = cmp<L>(c, b) > 0 ? v - T(0.5) * X : v + T(0.5) * X;
+            }
+        }
         break;
     } break;
     default:

@@ -7,11 +7,18 @@ namespace pl {
 // Collide kinds (one per reference collide routine; see include/panslbm_gb300.h).
 enum Kind {
     K_NS_COLLIDE = 0, K_NS_BRINKMAN = 1, K_AD_NATURAL = 2, K_AD_FORCE = 3, K_AD_HEATEX = 4,
-    K_AD_NATURAL_NOBRINK = 5, K_AD_FORCE_NOBRINK = 6,
-    K_ANS_BRINKMAN = 10, K_AAD_NATURAL = 11, K_AAD_FORCE = 12, K_AAD_HEATEX = 13, K_AAD_MASSFLOW = 14
+    K_AD_NATURAL_NOBRINK = 5, K_AD_FORCE_NOBRINK = 6, K_NSIN_COLLIDE = 7, K_NSIN_BRINKMAN = 8,
+    K_ANS_BRINKMAN = 10, K_AAD_NATURAL = 11, K_AAD_FORCE = 12, K_AAD_HEATEX = 13, K_AAD_MASSFLOW = 14,
+    K_ANSIN_BRINKMAN = 15
 };
 __host__ __device__ constexpr bool kind_is_adjoint(int k) { return k >= 10; }
-__host__ __device__ constexpr bool kind_has_g(int k) { return !(k == K_NS_COLLIDE || k == K_NS_BRINKMAN || k == K_ANS_BRINKMAN); }
+// the incompressible variants (NSin / ANSin), defined by the reference for D2Q9 only
+__host__ __device__ constexpr bool kind_incompressible(int k) {
+    return k == K_NSIN_COLLIDE || k == K_NSIN_BRINKMAN || k == K_ANSIN_BRINKMAN;
+}
+__host__ __device__ constexpr bool kind_has_g(int k) {
+    return !(k == K_NS_COLLIDE || k == K_NS_BRINKMAN || k == K_ANS_BRINKMAN || kind_incompressible(k));
+}
 __host__ __device__ constexpr bool kind_node_kappa(int k) {
     return k == K_AD_NATURAL || k == K_AD_FORCE || k == K_AAD_NATURAL || k == K_AAD_FORCE || k == K_AAD_MASSFLOW;
 }
@@ -26,7 +33,9 @@ __host__ __device__ constexpr bool kind_has_snapshot(int k) {
 // Boundary-program op kinds (same numbering as the oracle) plus smoothing.
 enum BcKind {
     BC_WALL = 0, BC_IWALL = 1, BC_NS_U = 2, BC_NS_RHO = 3, BC_AD_T = 4, BC_AD_Q = 5, BC_AD_QC = 6,
-    BC_ANS_U = 7, BC_ANS_RHO = 8, BC_AAD_T = 9, BC_AAD_Q = 10, BC_AAD_RHO = 11, BC_SMOOTH = 20
+    BC_ANS_U = 7, BC_ANS_RHO = 8, BC_AAD_T = 9, BC_AAD_Q = 10, BC_AAD_RHO = 11,
+    BC_NSIN_U = 12, BC_NSIN_RHO = 13, BC_ANSIN_U = 14,   // D2Q9 only
+    BC_SMOOTH = 20
 };
 
 // ops the interior kernel applies inline (walls, AD SetT / SetQ, AAD iSetT / iSetQ)

@@ -1,6 +1,7 @@
 // inst_body.cuh -- explicit kernel instantiations and launch switch for one
 // (lattice, storage) pair. Included by inst_<lattice>_<storage>.cu with PL_LAT, PL_STORE and
-// PL_NAME defined; PL_ALL_KINDS selects every collide kind (else the primary ones only).
+// PL_NAME defined; PL_ALL_KINDS selects every collide kind (else the primary ones only) and
+// PL_INCOMPRESSIBLE adds the D2Q9-only NSin / ANSin kinds.
 #include "kernels.cuh"
 #include "launch.h"
 
@@ -27,6 +28,11 @@ static __device__ __forceinline__ void collide_any(int kind, TC *f, TC *g, int i
     case K_ANS_BRINKMAN: collide_node<PL_LAT, TC, K_ANS_BRINKMAN>(f, g, idx, a, save, nullptr, a.geo.np, nullptr); break;
     case K_AAD_HEATEX: collide_node<PL_LAT, TC, K_AAD_HEATEX>(f, g, idx, a, save, nullptr, a.geo.np, nullptr); break;
     case K_AAD_MASSFLOW: collide_node<PL_LAT, TC, K_AAD_MASSFLOW>(f, g, idx, a, save, nullptr, a.geo.np, nullptr); break;
+#endif
+#if defined(PL_ALL_KINDS) && defined(PL_INCOMPRESSIBLE)
+    case K_NSIN_COLLIDE: collide_node<PL_LAT, TC, K_NSIN_COLLIDE>(f, g, idx, a, save, nullptr, a.geo.np, u); break;
+    case K_NSIN_BRINKMAN: collide_node<PL_LAT, TC, K_NSIN_BRINKMAN>(f, g, idx, a, save, nullptr, a.geo.np, u); break;
+    case K_ANSIN_BRINKMAN: collide_node<PL_LAT, TC, K_ANSIN_BRINKMAN>(f, g, idx, a, save, nullptr, a.geo.np, nullptr); break;
 #endif
     default: break;
     }
@@ -156,6 +162,11 @@ int PL_CAT(launch_, PL_NAME)(int kind, int op, bool save, const KArgs &a, cudaSt
     case K_ANS_BRINKMAN: run_kind<K_ANS_BRINKMAN>(op, save, a, st); return 0;
     case K_AAD_HEATEX: run_kind<K_AAD_HEATEX>(op, save, a, st); return 0;
     case K_AAD_MASSFLOW: run_kind<K_AAD_MASSFLOW>(op, save, a, st); return 0;
+#endif
+#if defined(PL_ALL_KINDS) && defined(PL_INCOMPRESSIBLE)
+    case K_NSIN_COLLIDE: run_kind<K_NSIN_COLLIDE>(op, save, a, st); return 0;
+    case K_NSIN_BRINKMAN: run_kind<K_NSIN_BRINKMAN>(op, save, a, st); return 0;
+    case K_ANSIN_BRINKMAN: run_kind<K_ANSIN_BRINKMAN>(op, save, a, st); return 0;
 #endif
     default: return -1;
     }

@@ -3,4 +3,5 @@
 #define PL_STORE double
 #define PL_NAME d2q9_f64
 #define PL_ALL_KINDS
+#define PL_INCOMPRESSIBLE
 #include "inst_body.cuh"

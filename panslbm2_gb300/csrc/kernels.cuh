@@ -274,7 +274,9 @@ __global__ void __launch_bounds__(128) k_stream_program(KArgs a, int has_g, int 
 
 // ---- equilibrium initial conditions (navierstokes.h:548-572, advection.h:1046-1070,
 //      adjointnavierstokes.h:472-498, adjointadvection.h:1357-1381) ---------------------------
-// which: 0 NS (rho,u), 1 AD (T,u), 2 ANS (ip,iu; u), 3 AAD (iT,iq; u). in[]: double fields.
+// which: 0 NS (rho,u), 1 AD (T,u), 2 ANS (ip,iu; u), 3 AAD (iT,iq; u), 4 NSin (rho,u),
+// 5 ANSin (ip,iu) (nsincompressible.h:202-212, adjointnsincompressible.h:180-192). in[]: double
+// fields.
 template <class L, class S>
 __global__ void k_init(KArgs a, int which, const double *in0, const double *in1, const double *in2,
                        const double *in3, const double *ux, const double *uy, const double *uz) {
@@ -298,6 +300,14 @@ __global__ void k_init(KArgs a, int which, const double *in0, const double *in1,
         const T iu[3] = {T(in1[idx]), T(in2[idx]), L::ND == 3 ? T(in3[idx]) : T(0)};
 #pragma unroll
         for (int c = 0; c < Q; ++c) eq[c] = ans_feq<L, T>(c, u, T(in0[idx]), iu);
+    } else if (which == 4) {
+        const T rhouu = T(in0[idx]) - T(1.5) * (u[0] * u[0] + u[1] * u[1]);
+#pragma unroll
+        for (int c = 0; c < Q; ++c) eq[c] = nsin_feq<L, T>(c, u, rhouu);
+    } else if (which == 5) {
+        const T iu[3] = {T(in1[idx]), T(in2[idx]), T(0)};
+#pragma unroll
+        for (int c = 0; c < Q; ++c) eq[c] = ansin_feq<L, T>(c, T(in0[idx]), iu);
     } else {
         const T iq[3] = {T(in1[idx]), T(in2[idx]), L::ND == 3 ? T(in3[idx]) : T(0)};
         const T v = T(in0[idx]) + T(3) * vdot<L, T>(u, iq);

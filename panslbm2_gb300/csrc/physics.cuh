@@ -186,7 +186,102 @@ template <class L, class T> __device__ __forceinline__ void aad_massflow(T *f, T
     }
 }
 
+// ---- incompressible variants (D2Q9) -------------------------------------------------------
+// NSin::Macro (nsincompressible.h:13-25): rho and the momentum sums, without the division by rho
+template <class L, class T> __device__ __forceinline__ void nsin_macro(const T *f, T &rho, T *u) {
+    T r = f[0], m0 = T(0), m1 = T(0);
+#pragma unroll
+    for (int c = 1; c < L::Q; ++c) {
+        const T v = f[c];
+        r += v;
+        if (L::cx(c) == 1) m0 += v; else if (L::cx(c) == -1) m0 -= v;
+        if (L::cy(c) == 1) m1 += v; else if (L::cy(c) == -1) m1 -= v;
+    }
+    rho = r;
+    u[0] = m0; u[1] = m1; u[2] = T(0);
+}
+// NSin::Equilibrium (nsincompressible.h:27-35); rhouu = rho - 1.5 u.u
+template <class L, class T> __device__ __forceinline__ T nsin_feq(int c, const T *u, T rhouu) {
+    const T ciu = cdot<L, T>(c, u[0], u[1], T(0));
+    return wt<L, T>(c) * (T(3) * ciu + T(4.5) * ciu * ciu + rhouu);
+}
+// ANSin::Macro (adjointnsincompressible.h:13-30)
+template <class L, class T> __device__ __forceinline__ void ansin_macro(const T *f, const T *u, T &ip, T *iu, T *im) {
+    const T w0 = wt<L, T>(0);
+    ip = f[0] * w0;
+    iu[0] = -f[0] * w0 * u[0]; iu[1] = -f[0] * w0 * u[1];
+    im[0] = T(0); im[1] = T(0);
+#pragma unroll
+    for (int c = 1; c < L::Q; ++c) {
+        const T ciu = cdot<L, T>(c, u[0], u[1], T(0));
+        const T fei = f[c] * wt<L, T>(c);
+        ip += fei;
+#pragma unroll
+        for (int b = 0; b < 2; ++b) {
+            const T cb = T(comp<L>(c, b));
+            iu[b] += fei * (cb + T(3) * ciu * cb - u[b]);
+        }
+#pragma unroll
+        for (int b = 0; b < 2; ++b) {
+            const int cb = comp<L>(c, b);
+            if (cb == 1) im[b] += fei; else if (cb == -1) im[b] -= fei;
+        }
+    }
+    iu[2] = T(0); im[2] = T(0);
+}
+// ANSin::Equilibrium (adjointnsincompressible.h:32-38)
+template <class L, class T> __device__ __forceinline__ T ansin_feq(int c, T ip, const T *iu) {
+    return ip + T(3) * cdot<L, T>(c, iu[0], iu[1], T(0));
+}
+// ANSin::ExternalForceBrinkman (adjointnsincompressible.h:40-47)
+template <class L, class T> __device__ __forceinline__ void ansin_brinkman(T *f, const T *im, T alpha) {
+    const T coef = T(3) * alpha / (T(1) + alpha);
+#pragma unroll
+    for (int c = 1; c < L::Q; ++c) f[c] -= coef * cdot<L, T>(c, im[0], im[1], T(0));
+}
+
 template <class T> __device__ __forceinline__ T ldT(const void *p, int idx) { return static_cast<const T *>(p)[idx]; }
+
+// NSin::MacroCollide / MacroBrinkmanCollide (nsincompressible.h:144-200) and
+// ANSin::MacroBrinkmanCollide (adjointnsincompressible.h:143-178) for one node
+template <class L, class T, int K>
+__device__ __forceinline__ void collide_incompressible(T *f, int idx, const KArgs &a, bool save, T *uout) {
+    constexpr int Q = L::Q;
+    const T omf = T(1) / (T(3) * T(a.ph.nu) + T(0.5));
+    const T iomf = T(1) - omf;
+    if (K == K_NSIN_COLLIDE || K == K_NSIN_BRINKMAN) {
+        T rho, u[3];
+        nsin_macro<L, T>(f, rho, u);
+        if (K == K_NSIN_BRINKMAN) {
+            ns_brinkman<L, T>(f, rho, u, ldT<T>(a.alpha, idx));
+            nsin_macro<L, T>(f, rho, u);
+        }
+        if (save) {
+            if (a.out[0]) a.out[0][idx] = double(rho);
+            if (a.out[1]) a.out[1][idx] = double(u[0]);
+            if (a.out[2]) a.out[2][idx] = double(u[1]);
+        }
+        if (uout) { uout[0] = u[0]; uout[1] = u[1]; uout[2] = T(0); }
+        const T rhouu = rho - T(1.5) * (u[0] * u[0] + u[1] * u[1]);
+#pragma unroll
+        for (int c = 0; c < Q; ++c) f[c] = iomf * f[c] + omf * nsin_feq<L, T>(c, u, rhouu);
+    } else {
+        const T u[3] = {ldT<T>(a.fwd[1], idx), ldT<T>(a.fwd[2], idx), T(0)};
+        T ip, iu[3], im[3];
+        ansin_macro<L, T>(f, u, ip, iu, im);
+        ansin_brinkman<L, T>(f, im, ldT<T>(a.alpha, idx));
+        ansin_macro<L, T>(f, u, ip, iu, im);
+        if (save) {
+            if (a.out[0]) a.out[0][idx] = double(ip);
+            if (a.out[1]) a.out[1][idx] = double(iu[0]);
+            if (a.out[2]) a.out[2][idx] = double(iu[1]);
+            if (a.out[4]) a.out[4][idx] = double(im[0]);
+            if (a.out[5]) a.out[5][idx] = double(im[1]);
+        }
+#pragma unroll
+        for (int c = 0; c < Q; ++c) f[c] = iomf * f[c] + omf * ansin_feq<L, T>(c, ip, iu);
+    }
+}
 
 // Macro + forces + BGK for one node, one reference collide routine per kind:
 // NS::MacroCollide / MacroBrinkmanCollide (navierstokes.h:430-546); AD::MacroCollide{Force,
@@ -199,6 +294,10 @@ template <class T> __device__ __forceinline__ T ldT(const void *p, int idx) { re
 template <class L, class T, int K>
 __device__ __forceinline__ void collide_node(T *f, T *g, int idx, const KArgs &a, bool save, double *snap,
                                              long long np, T *uout) {
+    if constexpr (kind_incompressible(K)) {
+        collide_incompressible<L, T, K>(f, idx, a, save, uout);
+        return;
+    }
     constexpr int Q = L::Q;
     const T omf = T(1) / (T(3) * T(a.ph.nu) + T(0.5));
     T omg = T(0);

@@ -3,7 +3,7 @@ import numpy as np
 
 from panslbm2_gb300 import _capi as A
 
-F_KINDS = (A.BC_NS_U, A.BC_NS_RHO, A.BC_ANS_U, A.BC_ANS_RHO, A.BC_AAD_RHO)
+F_KINDS = (A.BC_NS_U, A.BC_NS_RHO, A.BC_ANS_U, A.BC_ANS_RHO, A.BC_AAD_RHO, A.BC_NSIN_U, A.BC_NSIN_RHO, A.BC_ANSIN_U)
 
 
 def replay(o, L, f, g, ops, n, ux=None, uy=None, uz=None, rho=None, tem=None, kappa=None):

@@ -10,12 +10,15 @@ library. Reference routines per case:
   stream   D2Q9::Stream / iStream (d2q9.h:165-427), D3Q15::Stream / iStream (d3q15.h:256-980)
   bc       every edge/face routine of one kind on all edges/faces and two interior lines
            (d2q9.h:429-575, d3q15.h:982-1239, navierstokes.h:91-426, advection.h:98-524,
-           adjointnavierstokes.h:97-392, adjointadvection.h:154-751)
+           adjointnavierstokes.h:97-392, adjointadvection.h:154-751; on D2Q9 also
+           nsincompressible.h:46-140, adjointnsincompressible.h:49-92)
   smooth   SmoothCorner, SmoothCornerAt, SmoothCornerAlong{YZ,ZX,XY} (d2q9.h:577-587,
            d3q15.h:1241-1303)
   collide  the twelve Macro*Collide* routines with save (navierstokes.h:430-546,
            advection.h:528-1044, adjointnavierstokes.h:396-470, adjointadvection.h:892-1355)
-  init     NS / AD / ANS / AAD InitialCondition
+           and, on D2Q9, the three incompressible ones (nsincompressible.h:144-200,
+           adjointnsincompressible.h:143-178)
+  init     NS / AD / ANS / AAD InitialCondition; NSin / ANSin on D2Q9
   sens     the four sensitivity routines (adjointadvection.h:1443-1543,
            adjointnavierstokes.h:540-554)
   filter   HeavisideFilter::GetFilteredVariable / GetFilteredSensitivity, DensityFilter
@@ -24,6 +27,8 @@ library. Reference routines per case:
            calls, SmoothCorner; T steps from a perturbed equilibrium
   hsadj    the adjoint driver loop (heatsink.cpp:181-212) from the hsfwd state, then the
            four sensitivities
+  nsinch   an incompressible Brinkman channel on D2Q9: NSin forward steps (walls, NSin velocity
+           inlet and pressure outlet), ANSin adjoint steps, the Brinkman sensitivity
 """
 import zlib
 
@@ -39,10 +44,14 @@ FILTER_SHAPES = {"q9": (9, 13, 11, 1), "q15": (15, 7, 8, 6)}
 HS_SHAPES = {"q9": (2, 16, 12, 1), "q15": (3, 8, 9, 7)}
 FWD = ["NS_COLLIDE", "NS_BRINKMAN", "AD_NATURAL", "AD_FORCE", "AD_HEATEX", "AD_NATURAL_NOBRINK", "AD_FORCE_NOBRINK"]
 ADJ = ["ANS_BRINKMAN", "AAD_NATURAL", "AAD_FORCE", "AAD_HEATEX", "AAD_MASSFLOW"]
+# the incompressible variants exist for D2Q9 only
+FWD_IN, ADJ_IN = ["NSIN_COLLIDE", "NSIN_BRINKMAN"], ["ANSIN_BRINKMAN"]
+NO_G = ("NS_COLLIDE", "NS_BRINKMAN", "ANS_BRINKMAN", "NSIN_COLLIDE", "NSIN_BRINKMAN", "ANSIN_BRINKMAN")
 FWD_NAMES = ["rho", "ux", "uy", "uz", "tem", "qx", "qy", "qz"]
 ADJ_NAMES = ["ip", "iux", "iuy", "iuz", "imx", "imy", "imz", "item", "iqx", "iqy", "iqz"]
 BC_KINDS = ["WALL", "IWALL", "NS_U", "NS_RHO", "AD_T", "AD_Q", "AD_QC", "ANS_U", "ANS_RHO", "AAD_T", "AAD_Q",
-            "AAD_RHO"]
+            "AAD_RHO", "NSIN_U", "NSIN_RHO", "ANSIN_U"]
+BC_2D_ONLY = ("NSIN_U", "NSIN_RHO", "ANSIN_U")
 PH = dict(nu=0.1, diff=0.02, gx=0.001, gy=-0.002, gz=0.0015, tem0=0.3)
 HS_FWD_STEPS, HS_ADJ_STEPS = 25, 20
 
@@ -95,7 +104,7 @@ def bc_inputs(name, sk, kind):
     return dict(shape=np.array([q, nx, ny, nz]), kind=np.array(BC_KINDS.index(kind)),
                 lat=np.array(int(rng.integers(0, 2)) if kind in ("WALL", "IWALL") else 0),
                 f=pops(rng, q, n), g=pops(rng, q, n, base=0.5), type=ty,
-                v0=field(rng, n, 0.9, 1.1) if kind not in ("NS_U", "ANS_U") else field(rng, n, -0.05, 0.05),
+                v0=field(rng, n, 0.9, 1.1) if kind not in ("NS_U", "ANS_U", "NSIN_U") else field(rng, n, -0.05, 0.05),
                 v1=field(rng, n, -0.05, 0.05), v2=field(rng, n, -0.05, 0.05), ux=field(rng, n, -0.05, 0.05),
                 uy=field(rng, n, -0.05, 0.05), uz=field(rng, n, -0.05, 0.05), rho=field(rng, n, 0.95, 1.05),
                 tem=field(rng, n, 0, 1), kap=field(rng, n, 0.01, 0.2))
@@ -155,7 +164,7 @@ def collide_inputs(name, sk, kind):
     n = nx * ny * nz
     rng = _rng(name)
     d = design_inputs(rng, n)
-    has_g = kind not in ("NS_COLLIDE", "NS_BRINKMAN", "ANS_BRINKMAN")
+    has_g = kind not in NO_G
     d.update(shape=np.array([q, nx, ny, nz]), kind=np.array(getattr(A, kind)), f=pops(rng, q, n),
              g=pops(rng, q, n, base=0.5) if has_g else np.zeros((0,)))
     return d
@@ -369,6 +378,73 @@ def hsadj_run(lib, inp):
     return out
 
 
+# ---------------------------------------------------------------------------- incompressible channel
+NSIN_SHAPE = (9, 20, 12, 1)
+NSIN_FWD_STEPS, NSIN_ADJ_STEPS = 30, 25
+
+
+def nsin_program(kind, nx, ny, uin):
+    """Walls on the y edges, velocity inlet on x = 0, pressure outlet on x = nx-1 (forward); the
+    matching adjoint calls (iBoundaryCondition walls, ANSin::iBoundaryConditionSetU,
+    ANS::iBoundaryConditionSetRho, which ANSin reuses)."""
+    n = nx * ny
+    if kind == "forward":
+        return [dict(kind=A.BC_WALL, lat=0, axis=1, pos=0, dir=-1), dict(kind=A.BC_WALL, lat=0, axis=1, pos=ny - 1, dir=1),
+                dict(kind=A.BC_NSIN_U, axis=0, pos=0, dir=-1, v0=uin, v1=np.zeros(n)),
+                dict(kind=A.BC_NSIN_RHO, axis=0, pos=nx - 1, dir=1, c0=1.0, c1=0.0)]
+    return [dict(kind=A.BC_IWALL, lat=0, axis=1, pos=0, dir=-1), dict(kind=A.BC_IWALL, lat=0, axis=1, pos=ny - 1, dir=1),
+            dict(kind=A.BC_ANSIN_U, axis=0, pos=0, dir=-1, eps=0.3),
+            dict(kind=A.BC_ANS_RHO, axis=0, pos=nx - 1, dir=1)]
+
+
+def nsin_inputs(name):
+    q, nx, ny, nz = NSIN_SHAPE
+    n = nx * ny
+    rng = _rng(name)
+    jj = np.repeat(np.arange(ny), nx).astype(np.float64)
+    uin = 0.02 * 4.0 * jj * (ny - 1 - jj) / (ny - 1) ** 2
+    return dict(alpha=field(rng, n, 0.0, 0.1), dads=field(rng, n, -1, 1), uin=uin,
+                rho0=1.0 + 0.01 * rng.standard_normal(n), ux0=0.01 * rng.standard_normal(n),
+                uy0=0.01 * rng.standard_normal(n), ip0=0.01 * rng.standard_normal(n),
+                iux0=0.01 * rng.standard_normal(n), iuy0=0.01 * rng.standard_normal(n))
+
+
+def nsin_run(lib, inp):
+    """NSin::MacroBrinkmanCollide, Stream and the forward boundary calls for NSIN_FWD_STEPS, then
+    ANSin::MacroBrinkmanCollide, iStream and the adjoint calls for NSIN_ADJ_STEPS, then
+    ANSin::SensitivityBrinkman (the ANS routine)."""
+    q, nx, ny, nz = NSIN_SHAPE
+    n = nx * ny
+    L = lib.lat(q, nx, ny, 1)
+    ph = dict(nu=0.1, diff=0.0, gx=0.0, gy=0.0, gz=0.0, tem0=0.0)
+    f = np.zeros((q, n))
+    lib.init(L, 4, f, lib.fields(rho=inp["rho0"], ux=inp["ux0"], uy=inp["uy0"]))
+    mac = {nm: np.zeros(n) for nm in ("rho", "ux", "uy")}
+    ops = nsin_program("forward", nx, ny, inp["uin"])
+    for t in range(1, NSIN_FWD_STEPS + 1):
+        lib.collide(L, A.NSIN_BRINKMAN, f, None, lib.fields(alpha=inp["alpha"], **mac), **ph, save=True)
+        if t == NSIN_FWD_STEPS:
+            break
+        lib.stream(L, f)
+        replay(lib, L, f, None, ops, n)
+    fa = np.zeros((q, n))
+    lib.init(L, 5, fa, lib.fields(ux=mac["ux"], uy=mac["uy"], ip=inp["ip0"], iux=inp["iux0"], iuy=inp["iuy0"]))
+    am = {nm: np.zeros(n) for nm in ("ip", "iux", "iuy", "imx", "imy")}
+    ops = nsin_program("adjoint", nx, ny, inp["uin"])
+    for t in range(1, NSIN_ADJ_STEPS + 1):
+        lib.collide(L, A.ANSIN_BRINKMAN, fa, None, lib.fields(alpha=inp["alpha"], **mac, **am), **ph, save=True)
+        if t == NSIN_ADJ_STEPS:
+            break
+        lib.stream(L, fa, True)
+        replay(lib, L, fa, None, ops, n)
+    s = np.zeros(n)
+    lib.sensitivity(L, 3, s, lib.fields(ux=mac["ux"], uy=mac["uy"], imx=am["imx"], imy=am["imy"]), inp["dads"])
+    out = dict(f=f, fa=fa, sens=s)
+    out.update({"m_" + k: v for k, v in mac.items()})
+    out.update({"m_" + k: v for k, v in am.items()})
+    return out
+
+
 # ---------------------------------------------------------------------------- registry
 def all_cases():
     """name -> (make_inputs, run)."""
@@ -380,16 +456,19 @@ def all_cases():
         for kind in BC_KINDS:
             if kind == "AAD_RHO" and sk == "q15":
                 continue   # the reference's D3Q15 iBoundaryConditionSetRho overloads do not compile
+            if kind in BC_2D_ONLY and sk == "q15":
+                continue
             nm = "bc_%s_%s" % (sk, kind)
             cases[nm] = (lambda nm=nm, sk=sk, kind=kind: bc_inputs(nm, sk, kind), bc_run)
         nm = "smooth_%s" % sk
         cases[nm] = (lambda nm=nm, sk=sk: smooth_inputs(nm, sk), smooth_run)
-        for kind in FWD + ADJ:
+        for kind in FWD + ADJ + (FWD_IN + ADJ_IN if sk == "q9" else []):
             nm = "collide_%s_%s" % (sk, kind)
             cases[nm] = (lambda nm=nm, sk=sk, kind=kind: collide_inputs(nm, sk, kind), collide_run)
-        for which in range(4):
+        for which in range(6 if sk == "q9" else 4):
             nm = "init_%s_%d" % (sk, which)
             cases[nm] = (lambda nm=nm, sk=sk, w=which: init_inputs(nm, sk, w), init_run)
+        for which in range(4):
             nm = "sens_%s_%d" % (sk, which)
             cases[nm] = (lambda nm=nm, sk=sk, w=which: sens_inputs(nm, sk, w), sens_run)
         for R in (1.5, 3.0):
@@ -400,6 +479,7 @@ def all_cases():
         cases[nm] = (lambda nm=nm, sk=sk: hs_inputs(nm, sk), hsfwd_run)
         nm = "hsadj_%s" % sk
         cases[nm] = (lambda nm=nm, sk=sk: hs_inputs(nm, sk), hsadj_run)
+    cases["nsinch_q9"] = (lambda: nsin_inputs("nsinch_q9"), nsin_run)
     for nc in (1, 2, 3):
         nm = "resid_%d" % nc
         cases[nm] = (lambda nm=nm, nc=nc: resid_inputs(nm, nc), resid_run)

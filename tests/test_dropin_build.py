@@ -29,8 +29,9 @@ def _compile(src, out, extra=()):
     assert p.returncode == 0, p.stderr[-4000:]
 
 
-def test_heatsink_driver_builds(tmp_path):
-    _compile(os.path.join(ROOT, "tests", "dropin", "heatsink_driver.cpp"), str(tmp_path / "heatsink_driver"))
+@pytest.mark.parametrize("driver", ["heatsink_driver", "nsin_channel_driver"])
+def test_test_driver_builds(tmp_path, driver):
+    _compile(os.path.join(ROOT, "tests", "dropin", driver + ".cpp"), str(tmp_path / driver))
 
 
 @pytest.mark.skipif(obuild.reference_root() is None, reason="reference sources not present")

@@ -86,3 +86,43 @@ def test_dropin_adjoint_loop_and_sensitivities(driver, tmp_path, path):
     sens = rest[11 * n:].reshape(4, n)
     for w in range(4):
         close(sens[w], out["sens%d" % w], 1e-10)
+
+
+@pytest.fixture(scope="module")
+def nsin_driver(tmp_path_factory):
+    cxx = shutil.which("g++")
+    if cxx is None:
+        pytest.skip("g++ not found")
+    out = str(tmp_path_factory.mktemp("dropin") / "nsin_channel_driver")
+    cmd = [cxx, "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"),
+           os.path.join(ROOT, "tests", "dropin", "nsin_channel_driver.cpp"), "-L", LIBDIR, "-lpanslbm_gb300",
+           "-Wl,-rpath," + LIBDIR, "-o", out]
+    subprocess.check_call(cmd)
+    return out
+
+
+def test_dropin_incompressible_channel(nsin_driver, tmp_path):
+    """NSin forward + ANSin adjoint + the Brinkman sensitivity written against the template API
+    reproduce the reference's own loop (tests/golden/nsinch_q9.npz)."""
+    inp, out = C.load(os.path.join(ROOT, "tests", "golden", "nsinch_q9.npz"))
+    q, nx, ny, _ = C.NSIN_SHAPE
+    n = nx * ny
+    fin, fout = tmp_path / "in.bin", tmp_path / "out.bin"
+    with open(fin, "wb") as fh:
+        fh.write(struct.pack("4i", nx, ny, C.NSIN_FWD_STEPS, C.NSIN_ADJ_STEPS))
+        fh.write(struct.pack("2d", 0.1, 0.3))
+        for nm in ("alpha", "dads", "uin", "rho0", "ux0", "uy0", "ip0", "iux0", "iuy0"):
+            fh.write(np.ascontiguousarray(inp[nm], np.float64).tobytes())
+    subprocess.check_call([nsin_driver, str(fin), str(fout)])
+    got = np.fromfile(fout, np.float64)
+    close(got[:q * n], out["f"], 1e-11)
+    o = q * n
+    for nm in ("rho", "ux", "uy"):
+        close(got[o:o + n], out["m_" + nm], 1e-11)
+        o += n
+    close(got[o:o + q * n], out["fa"], 1e-11)
+    o += q * n
+    for nm in ("ip", "iux", "iuy", "imx", "imy"):
+        close(got[o:o + n], out["m_" + nm], 1e-11)
+        o += n
+    close(got[o:o + n], out["sens"], 1e-10)
