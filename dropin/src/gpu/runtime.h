@@ -465,9 +465,10 @@ struct Pair {
     //  one collide of the reference; outs: the host arrays the routine saves into
     template <class T>
     void collide(int kind, const pl_phys &ph, bool save, T *const *outs, int nouts, T *snap) {
-        const bool adjoint = kind >= PL_ANS_BRINKMAN;
+        const bool adjoint = (kind >= PL_ANS_BRINKMAN && kind <= PL_ANSIN_BRINKMAN) || kind == PL_AEL_COLLIDE;
         const bool has_g = !(kind == PL_NS_COLLIDE || kind == PL_NS_BRINKMAN || kind == PL_ANS_BRINKMAN ||
-                             kind == PL_NSIN_COLLIDE || kind == PL_NSIN_BRINKMAN || kind == PL_ANSIN_BRINKMAN);
+                             kind == PL_NSIN_COLLIDE || kind == PL_NSIN_BRINKMAN || kind == PL_ANSIN_BRINKMAN ||
+                             kind == PL_EL_COLLIDE || kind == PL_EL_EXTENDED || kind == PL_AEL_COLLIDE);
         const int slot = adjoint ? 1 : 0;
         const bool saves_snap = save && snap != nullptr;
         std::vector<int> idx;
@@ -746,11 +747,32 @@ const std::vector<int> &filter_mask(const Pair &pr, double R, const F &w) {
 
 template <class T>
 pl_phys phys(T nu, T diff, T gx, T gy, T gz, T tem0) {
-    pl_phys ph;
+    pl_phys ph{};
     ph.nu = double(nu); ph.diff = double(diff); ph.gx = double(gx); ph.gy = double(gy); ph.gz = double(gz);
     ph.tem0 = double(tem0);
     return ph;
 }
+
+//  the elastic kinds relax at 1 / tau
+template <class T>
+pl_phys phys_tau(T tau) {
+    pl_phys ph{};
+    ph.tau = double(tau);
+    return ph;
+}
+
+//  A caller's node array read as a functor of (i, j[, k]) (local = global coordinates on one
+//  device). It holds a shared_ptr, so it is not trivially copyable and record_bc evaluates it
+//  afresh on every call: the caller may rewrite the array between calls.
+template <class T>
+struct NodeValues {
+    const T *p;
+    int nx, ny;
+    std::shared_ptr<int> fresh = std::make_shared<int>(0);
+    NodeValues(const T *p_, int nx_, int ny_) : p(p_), nx(nx_), ny(ny_) {}
+    double operator()(int i, int j) const { return double(p[i + (size_t)nx * j]); }
+    double operator()(int i, int j, int k) const { return double(p[i + (size_t)nx * (j + (size_t)ny * k)]); }
+};
 
 }  // namespace gpu
 }  // namespace PANSLBM2

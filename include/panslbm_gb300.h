@@ -55,6 +55,9 @@ extern "C" {
 #define PL_AAD_HEATEX 13          /* AAD::MacroBrinkmanCollideHeatExchange    adjointadvection.h:892-993 */
 #define PL_AAD_MASSFLOW 14        /* AAD::MacroBrinkmanCollideNaturalConvectionMassFlow adjointadvection.h:1232-1355 */
 #define PL_ANSIN_BRINKMAN 15      /* ANSin::MacroBrinkmanCollide (D2Q9)       adjointnsincompressible.h:143-178 */
+#define PL_EL_COLLIDE 16          /* EL::MacroCollide (D2Q9; rate 1/tau)      elastic.h:109-136        */
+#define PL_EL_EXTENDED 17         /* EL::MacroExtendedCollide (D2Q9)          elastic.h:138-166        */
+#define PL_AEL_COLLIDE 18         /* AEL::MacroCollide (D2Q9; adjoint)        adjointelastic.h:96-125  */
 
 /* boundary-program op kinds */
 #define PL_BC_WALL 0      /* (D2Q9|D3Q15)::BoundaryConditionAlong*   type: 1 BARRIER, 2 MIRROR  */
@@ -73,6 +76,9 @@ extern "C" {
 #define PL_BC_NSIN_RHO 13 /* NSin::BoundaryConditionSetRhoAlong{X,Y}Edge v0 = rho, v1 = us      */
 #define PL_BC_ANSIN_U 14  /* ANSin::iBoundaryConditionSetUAlong{X,Y}Edge `eps`; ANSin's iSetRho
                            * is ANS's (PL_BC_ANS_RHO)                                            */
+#define PL_BC_EL_STRESS 15  /* EL::BoundaryConditionSetStressAlong{X,Y}Edge   v0,v1 = tx,ty (D2Q9) */
+#define PL_BC_AEL_STRESS 16 /* AEL::iBoundaryConditionSetStressAlong{X,Y}Edge v0,v1 = tx,ty,
+                             * v2 = the rho argument (D2Q9)                                       */
 #define PL_SMOOTH_CORNER 20  /* SmoothCorner()                                                   */
 #define PL_SMOOTH_AT 21      /* SmoothCornerAt(i,j[,k],di,dj[,dk])                               */
 #define PL_SMOOTH_LINE 22    /* SmoothCornerAlong{YZ,ZX,XY}: axis = 0,1,2; (i,j) = line, (di,dj)  */
@@ -84,6 +90,8 @@ extern "C" {
 #define PL_DIRX 3    /* mass-flow objective weights                 */
 #define PL_DIRY 4
 #define PL_DIRZ 5
+#define PL_DENSITY 6 /* EL density rho (the input array of the EL collides) */
+#define PL_GAMMA 7   /* EL / AEL stress scale gamma                 */
 #define PL_RHO 8     /* forward macros stored by the last saving collide */
 #define PL_UX 9
 #define PL_UY 10
@@ -103,6 +111,18 @@ extern "C" {
 #define PL_IQX 24
 #define PL_IQY 25
 #define PL_IQZ 26
+/* the elastic kinds store their macros in the planes above: EL ux, uy in PL_UX, PL_UY and the
+ * stress in the T / q planes; AEL irho in PL_IP, imx, imy in PL_IMX, PL_IMY and the adjoint
+ * stress in the adjoint T / q planes */
+#define PL_SXX PL_TEM
+#define PL_SXY PL_QX
+#define PL_SYX PL_QY
+#define PL_SYY PL_QZ
+#define PL_IRHO PL_IP
+#define PL_ISXX PL_ITEM
+#define PL_ISXY PL_IQX
+#define PL_ISYX PL_IQY
+#define PL_ISYY PL_IQZ
 #define PL_FWD_RHO 32   /* forward solution read by adjoint collides and adjoint BCs */
 #define PL_FWD_UX 33
 #define PL_FWD_UY 34
@@ -116,6 +136,7 @@ typedef struct {
     double diff;          /* constant diffusivity of the siblings that take one  */
     double gx, gy, gz;    /* buoyancy vector                                    */
     double tem0;          /* reference temperature                              */
+    double tau;           /* relaxation time of the EL / AEL kinds (rate 1/tau)  */
 } pl_phys;
 
 /* One boundary routine call, recorded in call order into a boundary program. Per-node
@@ -174,6 +195,11 @@ int pl_program_destroy(pl_lattice h, int prog);
 int pl_init(pl_lattice h, int which, const double *a0, const double *a1, const double *a2, const double *a3,
             const double *ux, const double *uy, const double *uz);
 
+/* elastic initial conditions (D2Q9): which 0 EL::InitialCondition (elastic.h:168-179), in = rho,
+ * ux, uy, sxx, sxy, syx, syy; 1 AEL::InitialCondition (adjointelastic.h:127-138), in = irho,
+ * imx, imy, isxx, isxy, isyx, isyy with gamma taken from PL_GAMMA. Seven host arrays of N. */
+int pl_init_elastic(pl_lattice h, int which, const double *const *in);
+
 /* one collide in place (the reference's Macro*Collide* call) */
 int pl_collide(pl_lattice h, int kind, const pl_phys *ph, int save);
 /* one fused step: Stream/iStream + program `prog` (-1: none) + collide of kind */
@@ -223,6 +249,11 @@ int pl_residual_device_noalloc(long long n, int ncomp, const double *const *a, c
  * reads PL_FWD_* (forward), the adjoint macros, PL_KAPPA and the two snapshots. */
 int pl_sensitivity(pl_lattice h, int which, double *dfds, const double *dads, const double *dkds, const double *qn,
                    const int *mask);
+
+/* AEL::SensitivityCompliance (adjointelastic.h:149-155), D2Q9: dfds (host, N) is accumulated
+ * into; in = nine host arrays sxx, sxy, syx, syy, irho, isxx, isxy, isyx, isyy, or NULL for the
+ * stress of the last saving EL collide and the adjoint of the last saving AEL collide. */
+int pl_sensitivity_compliance(pl_lattice h, double *dfds, const double *const *in);
 
 /* filters (heavisidefilter.h:404-899, densityfilter.h:10-515). mask: NULL = hat weight
  * everywhere; else hat weight between two design cells (mask != 0), identity otherwise. */

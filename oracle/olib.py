@@ -18,10 +18,12 @@ IP = C.POINTER(C.c_int)
 NS_COLLIDE, NS_BRINKMAN, AD_NATURAL, AD_FORCE, AD_HEATEX, AD_NATURAL_NOBRINK, AD_FORCE_NOBRINK = 0, 1, 2, 3, 4, 5, 6
 NSIN_COLLIDE, NSIN_BRINKMAN = 7, 8
 ANS_BRINKMAN, AAD_NATURAL, AAD_FORCE, AAD_HEATEX, AAD_MASSFLOW, ANSIN_BRINKMAN = 10, 11, 12, 13, 14, 15
+EL_COLLIDE, EL_EXTENDED, AEL_COLLIDE = 16, 17, 18
 # bc kinds
 BC_WALL, BC_IWALL, BC_NS_U, BC_NS_RHO, BC_AD_T, BC_AD_Q, BC_AD_QC = 0, 1, 2, 3, 4, 5, 6
 BC_ANS_U, BC_ANS_RHO, BC_AAD_T, BC_AAD_Q, BC_AAD_RHO = 7, 8, 9, 10, 11
 BC_NSIN_U, BC_NSIN_RHO, BC_ANSIN_U = 12, 13, 14
+BC_EL_STRESS, BC_AEL_STRESS = 15, 16
 
 
 class Lat(C.Structure):
@@ -30,7 +32,8 @@ class Lat(C.Structure):
 
 FIELD_NAMES = ["rho", "ux", "uy", "uz", "tem", "qx", "qy", "qz", "ip", "iux", "iuy", "iuz",
                "imx", "imy", "imz", "item", "iqx", "iqy", "iqz", "alpha", "diffusivity", "beta",
-               "dirx", "diry", "dirz", "gsnap"]
+               "dirx", "diry", "dirz", "gsnap", "sxx", "sxy", "syx", "syy", "isxx", "isxy", "isyx", "isyy",
+               "gamma"]
 
 
 class Fields(C.Structure):
@@ -39,7 +42,7 @@ class Fields(C.Structure):
 
 class Phys(C.Structure):
     _fields_ = [("nu", C.c_double), ("diff", C.c_double), ("gx", C.c_double), ("gy", C.c_double),
-                ("gz", C.c_double), ("tem0", C.c_double)]
+                ("gz", C.c_double), ("tem0", C.c_double), ("tau", C.c_double)]
 
 
 class BC(C.Structure):
@@ -122,8 +125,8 @@ class Oracle:
     def smooth_line(self, L, f, plane, a, b, da, db):
         self.lib.ol_smooth_line(C.byref(L), _dp(f), plane, a, b, da, db)
 
-    def collide(self, L, kind, f, g, F, nu, diff=0.0, gx=0.0, gy=0.0, gz=0.0, tem0=0.0, save=True):
-        P = Phys(nu, diff, gx, gy, gz, tem0)
+    def collide(self, L, kind, f, g, F, nu=0.0, diff=0.0, gx=0.0, gy=0.0, gz=0.0, tem0=0.0, save=True, tau=1.0):
+        P = Phys(nu, diff, gx, gy, gz, tem0, tau)
         self.lib.ol_collide(C.byref(L), int(kind), _dp(f), _dp(g), C.byref(F), C.byref(P), int(save))
 
     def init(self, L, which, f, F):

@@ -478,6 +478,61 @@ static void aad_node(const lat_t *t, int idx, int i, int j, int k, void *vctx) {
     (void)i; (void)j; (void)k;
 }
 
+/* ---- elastic stress BCs (D2Q9) ---------------------------------------------------------
+ * EL::BoundaryConditionSetStressAlong{X,Y}Edge (elastic.h:60-104): the three unknown
+ * populations from the known ones on the same node and the traction (tx, ty).
+ * AEL::iBoundaryConditionSetStressAlong{X,Y}Edge (adjointelastic.h:48-92): the three outgoing
+ * adjoint populations, with the traction divided by the node's density. The D2Q9 indices are
+ * spelled out as the reference does. */
+static void el_stress_node(const lat_t *t, int idx, int i, int j, int k, void *vctx) {
+    bcctx *x = (bcctx *)vctx;
+    const ol_bc *bc = x->bc;
+    if (!bc->type[idx]) return;
+    double *f = x->f;
+    const double tx = bc->v0[idx], ty = bc->v1[idx];
+#define E(c) F(f, c, idx)
+    if (bc->kind == OL_BC_EL_STRESS) {
+        if (bc->axis == 0 && bc->dir == -1) {
+            E(1) = E(3) - 4.0 * (E(3) + E(6) + E(7)) / 3.0 + 2.0 * tx / 3.0;
+            E(5) = E(6) - (E(3) + E(6) + E(7)) / 3.0 + (tx + 3.0 * ty) / 6.0;
+            E(8) = E(7) - (E(3) + E(6) + E(7)) / 3.0 + (tx - 3.0 * ty) / 6.0;
+        } else if (bc->axis == 0) {
+            E(3) = E(1) - 4.0 * (E(1) + E(5) + E(8)) / 3.0 - 2.0 * tx / 3.0;
+            E(6) = E(5) - (E(1) + E(5) + E(8)) / 3.0 - (tx - 3.0 * ty) / 6.0;
+            E(7) = E(8) - (E(1) + E(5) + E(8)) / 3.0 - (tx + 3.0 * ty) / 6.0;
+        } else if (bc->dir == -1) {
+            E(2) = E(4) - 4.0 * (E(4) + E(7) + E(8)) / 3.0 + 2.0 * ty / 3.0;
+            E(5) = E(8) - (E(4) + E(7) + E(8)) / 3.0 + (ty + 3.0 * tx) / 6.0;
+            E(6) = E(7) - (E(4) + E(7) + E(8)) / 3.0 + (ty - 3.0 * tx) / 6.0;
+        } else {
+            E(4) = E(2) - 4.0 * (E(2) + E(5) + E(6)) / 3.0 - 2.0 * ty / 3.0;
+            E(7) = E(6) - (E(2) + E(5) + E(6)) / 3.0 - (ty + 3.0 * tx) / 6.0;
+            E(8) = E(5) - (E(2) + E(5) + E(6)) / 3.0 - (ty - 3.0 * tx) / 6.0;
+        }
+    } else {
+        const double rho = bc->rho[idx];
+        if (bc->axis == 0 && bc->dir == -1) {
+            E(3) = E(1) - (4.0 * E(1) + E(5) + E(8)) / 3.0 + 2.0 * tx / rho;
+            E(6) = E(5) - (4.0 * E(1) + E(5) + E(8)) / 3.0 + 2.0 * (tx - ty) / rho;
+            E(7) = E(8) - (4.0 * E(1) + E(5) + E(8)) / 3.0 + 2.0 * (tx + ty) / rho;
+        } else if (bc->axis == 0) {
+            E(1) = E(3) - (4.0 * E(3) + E(6) + E(7)) / 3.0 - 2.0 * tx / rho;
+            E(5) = E(6) - (4.0 * E(3) + E(6) + E(7)) / 3.0 - 2.0 * (tx + ty) / rho;
+            E(8) = E(7) - (4.0 * E(3) + E(6) + E(7)) / 3.0 - 2.0 * (tx - ty) / rho;
+        } else if (bc->dir == -1) {
+            E(4) = E(2) - (4.0 * E(2) + E(5) + E(6)) / 3.0 + 2.0 * ty / rho;
+            E(7) = E(6) - (4.0 * E(2) + E(5) + E(6)) / 3.0 + 2.0 * (ty + tx) / rho;
+            E(8) = E(5) - (4.0 * E(2) + E(5) + E(6)) / 3.0 + 2.0 * (ty - tx) / rho;
+        } else {
+            E(2) = E(4) - (4.0 * E(4) + E(7) + E(8)) / 3.0 - 2.0 * ty / rho;
+            E(5) = E(8) - (4.0 * E(4) + E(7) + E(8)) / 3.0 - 2.0 * (ty + tx) / rho;
+            E(6) = E(7) - (4.0 * E(4) + E(7) + E(8)) / 3.0 - 2.0 * (ty - tx) / rho;
+        }
+    }
+#undef E
+    (void)t; (void)i; (void)j; (void)k;
+}
+
 void ol_apply_bc(const ol_lat *L, double *f, double *g, const ol_bc *bc) {
     lat_t T = mk(L); const lat_t *t = &T;
     bcctx x; x.bc = bc; x.f = f; x.g = g;
@@ -489,6 +544,7 @@ void ol_apply_bc(const ol_lat *L, double *f, double *g, const ol_bc *bc) {
     case OL_BC_ANS_U: case OL_BC_ANS_RHO: fn = ans_node; break;
     case OL_BC_AAD_T: case OL_BC_AAD_Q: case OL_BC_AAD_RHO: fn = aad_node; break;
     case OL_BC_NSIN_U: case OL_BC_NSIN_RHO: case OL_BC_ANSIN_U: if (t->nd != 2) return; fn = nsin_node; break;
+    case OL_BC_EL_STRESS: case OL_BC_AEL_STRESS: if (t->nd != 2) return; fn = el_stress_node; break;
     default: return;
     }
     for_face(t, bc->axis, bc->pos, fn, &x);
@@ -772,6 +828,63 @@ static void ansin_brinkman(const lat_t *t, double *f, const double *im, double a
     for (int c = 1; c < t->q; ++c) f[c] -= coef * (t->c[0][c] * im[0] + t->c[1][c] * im[1]);
 }
 
+/* ---- elastic LBM (D2Q9 only in the reference) ------------------------------------------- */
+/* EL::Macro (elastic.h:17-47): u = (sum_{c>=1} c f) / rho, s_ab = -sum_{c>=1} c_a c_b f; the
+ * topology-optimisation overload scales s by gamma. s = {sxx, sxy, syx, syy}. */
+static void el_macro(const lat_t *t, const double *f, double rho, double *u, double *s) {
+    double ux = 0.0, uy = 0.0, sxx = 0.0, sxy = 0.0, syx = 0.0, syy = 0.0;
+    for (int c = 1; c < t->q; ++c) {
+        const double v = f[c];
+        const int cx = t->c[0][c], cy = t->c[1][c];
+        ux += cx * v;
+        uy += cy * v;
+        sxx -= cx * cx * v;
+        sxy -= cx * cy * v;
+        syx -= cy * cx * v;
+        syy -= cy * cy * v;
+    }
+    const double invrho = 1.0 / rho;
+    u[0] = ux * invrho; u[1] = uy * invrho;
+    s[0] = sxx; s[1] = sxy; s[2] = syx; s[3] = syy;
+}
+/* EL::Equilibrium (elastic.h:49-58): w (3 rho c.u - 4.5 c.s.c + 1.5 tr s) */
+static void el_eq(const lat_t *t, double *feq, double rho, const double *u, const double *s) {
+    for (int c = 0; c < t->q; ++c) {
+        const int cx = t->c[0][c], cy = t->c[1][c];
+        const double ciu = cx * u[0] + cy * u[1];
+        const double cisci = cx * s[0] * cx + cx * s[1] * cy + cy * s[2] * cx + cy * s[3] * cy;
+        const double trss = s[0] + s[3];
+        feq[c] = t->w[c] * (3.0 * rho * ciu - 4.5 * cisci + 1.5 * trss);
+    }
+}
+/* AEL::Macro (adjointelastic.h:16-35): irho = sum w f, im = sum w c f, is_ab = sum w c_a c_b f.
+ * m = {irho, imx, imy, isxx, isxy, isyx, isyy} */
+static void ael_macro(const lat_t *t, const double *f, double *m) {
+    double irho = t->w[0] * f[0], imx = 0.0, imy = 0.0, isxx = 0.0, isxy = 0.0, isyx = 0.0, isyy = 0.0;
+    for (int c = 1; c < t->q; ++c) {
+        const double v = f[c], e = t->w[c];
+        const int cx = t->c[0][c], cy = t->c[1][c];
+        irho += e * v;
+        imx += e * cx * v;
+        imy += e * cy * v;
+        isxx += e * cx * cx * v;
+        isxy += e * cx * cy * v;
+        isyx += e * cy * cx * v;
+        isyy += e * cy * cy * v;
+    }
+    m[0] = irho; m[1] = imx; m[2] = imy; m[3] = isxx; m[4] = isxy; m[5] = isyx; m[6] = isyy;
+}
+/* AEL::Equilibrium (adjointelastic.h:37-46): 3 im.c + 4.5 gamma c.is.c - 1.5 gamma irho |c|^2 */
+static void ael_eq(const lat_t *t, double *feq, const double *m, double gamma) {
+    for (int c = 0; c < t->q; ++c) {
+        const int cx = t->c[0][c], cy = t->c[1][c];
+        const double imc = m[1] * cx + m[2] * cy;
+        const double cisc = cx * m[3] * cx + cx * m[4] * cy + cy * m[5] * cx + cy * m[6] * cy;
+        const double irhocc = m[0] * (cx * cx + cy * cy);
+        feq[c] = 3.0 * imc + 4.5 * gamma * cisc - 1.5 * gamma * irhocc;
+    }
+}
+
 /* ---- collide kernels ------------------------------------------------------------------
  * NS::MacroCollide / MacroBrinkmanCollide (navierstokes.h:430-546)
  * AD::MacroCollide{Force,Natural}Convection (advection.h:528-712),
@@ -780,7 +893,9 @@ static void ansin_brinkman(const lat_t *t, double *f, const double *im, double a
  * AAD::MacroBrinkmanCollide{HeatExchange,ForceConvection,NaturalConvection,
  *     NaturalConvectionMassFlow} (adjointadvection.h:892-1355)
  * NSin::MacroCollide / MacroBrinkmanCollide (nsincompressible.h:144-200),
- * ANSin::MacroBrinkmanCollide (adjointnsincompressible.h:143-178) */
+ * ANSin::MacroBrinkmanCollide (adjointnsincompressible.h:143-178)
+ * EL::MacroCollide / MacroExtendedCollide (elastic.h:109-166), AEL::MacroCollide
+ * (adjointelastic.h:96-125) */
 void ol_collide(const ol_lat *L, int kind, double *fa, double *ga, const ol_fields *Fd, const ol_phys *P, int save) {
     lat_t T = mk(L); const lat_t *t = &T;
     const int n = t->n, q = t->q, nd = t->nd;
@@ -797,7 +912,33 @@ void ol_collide(const ol_lat *L, int kind, double *fa, double *ga, const ol_fiel
             omg = 1.0 / (3.0 * Fd->diffusivity[idx] + 0.5);
         else if (ga)
             omg = 1.0 / (3.0 * P->diff + 0.5);
-        if (kind == OL_NSIN_COLLIDE || kind == OL_NSIN_BRINKMAN) {
+        if (kind == OL_EL_COLLIDE || kind == OL_EL_EXTENDED) {
+            /* EL::MacroCollide / MacroExtendedCollide (elastic.h:109-166), omega = 1 / tau */
+            const double rho = Fd->rho[idx], om = 1.0 / P->tau;
+            double u[2], sg[4];
+            el_macro(t, f, rho, u, sg);
+            if (kind == OL_EL_EXTENDED) {
+                const double gm = Fd->gamma[idx];
+                for (int m = 0; m < 4; ++m) sg[m] *= gm;
+            }
+            if (save) {
+                Fd->ux[idx] = u[0]; Fd->uy[idx] = u[1];
+                Fd->sxx[idx] = sg[0]; Fd->sxy[idx] = sg[1]; Fd->syx[idx] = sg[2]; Fd->syy[idx] = sg[3];
+            }
+            el_eq(t, feq, rho, u, sg);
+            bgk(t, f, feq, om);
+        } else if (kind == OL_AEL_COLLIDE) {
+            /* AEL::MacroCollide (adjointelastic.h:96-125) */
+            const double om = 1.0 / P->tau;
+            double m[7];
+            ael_macro(t, f, m);
+            if (save) {
+                Fd->ip[idx] = m[0]; Fd->imx[idx] = m[1]; Fd->imy[idx] = m[2];
+                Fd->isxx[idx] = m[3]; Fd->isxy[idx] = m[4]; Fd->isyx[idx] = m[5]; Fd->isyy[idx] = m[6];
+            }
+            ael_eq(t, feq, m, Fd->gamma[idx]);
+            bgk(t, f, feq, om);
+        } else if (kind == OL_NSIN_COLLIDE || kind == OL_NSIN_BRINKMAN) {
             double rho, u[3];
             nsin_macro(t, f, &rho, u);
             if (kind == OL_NSIN_BRINKMAN) {
@@ -896,13 +1037,28 @@ void ol_collide(const ol_lat *L, int kind, double *fa, double *ga, const ol_fiel
 
 /* ---- initial conditions: NS::InitialCondition (navierstokes.h:548-572), AD:: (advection.h:
  *      1046-1070), ANS:: (adjointnavierstokes.h:472-498), AAD:: (adjointadvection.h:1357-1381),
- *      NSin:: (nsincompressible.h:202-212), ANSin:: (adjointnsincompressible.h:180-192) */
+ *      NSin:: (nsincompressible.h:202-212), ANSin:: (adjointnsincompressible.h:180-192),
+ *      EL:: (elastic.h:168-179), AEL:: (adjointelastic.h:127-138) */
 void ol_init(const ol_lat *L, int which, double *fa, const ol_fields *Fd) {
     lat_t T = mk(L); const lat_t *t = &T;
     const int n = t->n, q = t->q, nd = t->nd;
 #pragma omp parallel for schedule(static)
     for (int idx = 0; idx < n; ++idx) {
         double eq[15];
+        if (which == 6) {
+            const double u[2] = {Fd->ux[idx], Fd->uy[idx]};
+            const double sg[4] = {Fd->sxx[idx], Fd->sxy[idx], Fd->syx[idx], Fd->syy[idx]};
+            el_eq(t, eq, Fd->rho[idx], u, sg);
+            for (int c = 0; c < q; ++c) fa[(size_t)c * n + idx] = eq[c];
+            continue;
+        }
+        if (which == 7) {
+            const double m[7] = {Fd->ip[idx], Fd->imx[idx], Fd->imy[idx], Fd->isxx[idx], Fd->isxy[idx],
+                                 Fd->isyx[idx], Fd->isyy[idx]};
+            ael_eq(t, eq, m, Fd->gamma[idx]);
+            for (int c = 0; c < q; ++c) fa[(size_t)c * n + idx] = eq[c];
+            continue;
+        }
         double u[3] = {Fd->ux[idx], Fd->uy[idx], nd == 3 ? Fd->uz[idx] : 0.0};
         if (which == 0) ns_eq(t, eq, Fd->rho[idx], u);
         else if (which == 1) ad_eq(t, eq, Fd->tem[idx], u);
@@ -933,6 +1089,14 @@ void ol_sensitivity(const ol_lat *L, int which, double *dfds, const ol_fields *F
                     const double *dkds, const double *g, const double *ig, const double *qn, const int *mask) {
     lat_t T = mk(L); const lat_t *t = &T;
     const int n = t->n, q = t->q, nd = t->nd;
+    if (which == 4) {
+        /* AEL::SensitivityCompliance (adjointelastic.h:149-155) */
+        for (int idx = 0; idx < n; ++idx)
+            dfds[idx] += (4.5 * (Fd->sxx[idx] * Fd->isxx[idx] + Fd->sxy[idx] * Fd->isxy[idx] +
+                                 Fd->syx[idx] * Fd->isyx[idx] + Fd->syy[idx] * Fd->isyy[idx]) -
+                          1.5 * Fd->ip[idx] * (Fd->sxx[idx] + Fd->syy[idx]));
+        return;
+    }
     for (int idx = 0; idx < n; ++idx) {
         double u[3] = {Fd->ux[idx], Fd->uy[idx], nd == 3 ? Fd->uz[idx] : 0.0};
         double im[3] = {Fd->imx[idx], Fd->imy[idx], nd == 3 ? Fd->imz[idx] : 0.0};

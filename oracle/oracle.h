@@ -37,6 +37,11 @@ typedef struct {
     const double *beta;                         /* heat-exchange coefficient beta[N]           */
     const double *dirx, *diry, *dirz;           /* mass-flow objective direction weights       */
     double *gsnap;                              /* g (fwd) / ig (adj) snapshot, snap[q*idx+c]  */
+    /* elastic kinds (D2Q9): EL reads rho as its density input and saves ux, uy and the stress
+     * sxx..syy; AEL saves irho in ip, imx / imy in imx / imy and the adjoint stress isxx..isyy */
+    double *sxx, *sxy, *syx, *syy;
+    double *isxx, *isxy, *isyx, *isyy;
+    const double *gamma;                        /* stress scale gamma[N] (EL extended, AEL)    */
 } ol_fields;
 
 typedef struct {
@@ -44,6 +49,7 @@ typedef struct {
     double diff;            /* constant diffusivity (siblings that take a scalar kappa) */
     double gx, gy, gz;      /* buoyancy vector                          */
     double tem0;            /* reference temperature                    */
+    double tau;             /* relaxation time of the elastic kinds     */
 } ol_phys;
 
 /* Collide kinds */
@@ -62,7 +68,10 @@ enum {
     OL_AAD_FORCE = 12,            /* AAD::MacroBrinkmanCollideForceConvection            */
     OL_AAD_HEATEX = 13,           /* AAD::MacroBrinkmanCollideHeatExchange               */
     OL_AAD_MASSFLOW = 14,         /* AAD::MacroBrinkmanCollideNaturalConvectionMassFlow  */
-    OL_ANSIN_BRINKMAN = 15        /* ANSin::MacroBrinkmanCollide (D2Q9)                  */
+    OL_ANSIN_BRINKMAN = 15,       /* ANSin::MacroBrinkmanCollide (D2Q9)                  */
+    OL_EL_COLLIDE = 16,           /* EL::MacroCollide (D2Q9)                             */
+    OL_EL_EXTENDED = 17,          /* EL::MacroExtendedCollide (D2Q9)                     */
+    OL_AEL_COLLIDE = 18           /* AEL::MacroCollide (D2Q9)                            */
 };
 
 /* Boundary-condition kinds applied along one edge (2D) / face (3D) */
@@ -81,8 +90,10 @@ enum {
     OL_BC_AAD_RHO = 11,   /* AAD::iBoundaryConditionSetRhoAlong* (type[]: 1 SetT, 2 SetQ; eps; acts on f and g) */
     OL_BC_NSIN_U = 12,    /* NSin::BoundaryConditionSetUAlong{X,Y}Edge   (v0,v1 = ux,uy)     */
     OL_BC_NSIN_RHO = 13,  /* NSin::BoundaryConditionSetRhoAlong{X,Y}Edge (v0 = rho, v1 = us) */
-    OL_BC_ANSIN_U = 14    /* ANSin::iBoundaryConditionSetUAlong{X,Y}Edge (eps); ANSin's iSetRho
+    OL_BC_ANSIN_U = 14,   /* ANSin::iBoundaryConditionSetUAlong{X,Y}Edge (eps); ANSin's iSetRho
                            * is ANS's (OL_BC_ANS_RHO)                                      */
+    OL_BC_EL_STRESS = 15, /* EL::BoundaryConditionSetStressAlong{X,Y}Edge   (v0,v1 = tx,ty)  */
+    OL_BC_AEL_STRESS = 16 /* AEL::iBoundaryConditionSetStressAlong{X,Y}Edge (v0,v1 = tx,ty; rho) */
 };
 
 typedef struct {
@@ -118,7 +129,8 @@ void ol_smooth_line(const ol_lat *L, double *f, int plane, int a, int b, int da,
 void ol_collide(const ol_lat *L, int kind, double *f, double *g, const ol_fields *F,
                 const ol_phys *P, int save);
 
-/* Initial conditions: 0 NS, 1 AD, 2 ANS, 3 AAD, 4 NSin (rho, u), 5 ANSin (ip, iu) */
+/* Initial conditions: 0 NS, 1 AD, 2 ANS, 3 AAD, 4 NSin (rho, u), 5 ANSin (ip, iu),
+ * 6 EL (rho, u, sxx..syy), 7 AEL (irho = ip, imx, imy, isxx..isyy, gamma) */
 void ol_init(const ol_lat *L, int which, double *f, const ol_fields *F);
 
 /* Sensitivities.
@@ -126,6 +138,7 @@ void ol_init(const ol_lat *L, int which, double *f, const ol_fields *F);
  *   which 1: AAD::SensitivityBrinkmanDiffusivity
  *   which 2: AAD::SensitivityHeatExchange (dkds = dbds)
  *   which 3: ANS::SensitivityBrinkman
+ *   which 4: AEL::SensitivityCompliance (stress sxx..syy, irho = ip, isxx..isyy; D2Q9)
  * g, ig: snapshots in snap[q*idx+c] layout. */
 void ol_sensitivity(const ol_lat *L, int which, double *dfds, const ol_fields *F,
                     const double *dads, const double *dkds, const double *g, const double *ig,

@@ -25,6 +25,8 @@
 #if REF_DIM == 2
 #include "src/equation/nsincompressible.h"
 #include "src/equation/adjointnsincompressible.h"
+#include "src/equation/elastic.h"
+#include "src/equation/adjointelastic.h"
 #endif
 #include "src/utility/heavisidefilter.h"
 #include "src/utility/densityfilter.h"
@@ -103,6 +105,8 @@ extern "C" void NAME(apply_bc)(const ol_lat *L, double *f, double *g, const ol_b
     case OL_BC_NSIN_U: if (a == 0) NSin::BoundaryConditionSetUAlongXEdge(*p, pos, d, V0, V1, T); else NSin::BoundaryConditionSetUAlongYEdge(*p, pos, d, V0, V1, T); break;
     case OL_BC_NSIN_RHO: if (a == 0) NSin::BoundaryConditionSetRhoAlongXEdge(*p, pos, d, V0, V1, T); else NSin::BoundaryConditionSetRhoAlongYEdge(*p, pos, d, V0, V1, T); break;
     case OL_BC_ANSIN_U: if (a == 0) ANSin::iBoundaryConditionSetUAlongXEdge(*p, pos, d, T, bc->eps); else ANSin::iBoundaryConditionSetUAlongYEdge(*p, pos, d, T, bc->eps); break;
+    case OL_BC_EL_STRESS: if (a == 0) EL::BoundaryConditionSetStressAlongXEdge(*p, pos, d, V0, V1, T); else EL::BoundaryConditionSetStressAlongYEdge(*p, pos, d, V0, V1, T); break;
+    case OL_BC_AEL_STRESS: if (a == 0) AEL::iBoundaryConditionSetStressAlongXEdge(*p, pos, d, V0, V1, bc->rho, T); else AEL::iBoundaryConditionSetStressAlongYEdge(*p, pos, d, V0, V1, bc->rho, T); break;
     }
 #else
     auto T = FI(ty[NID(i, j, k)]);
@@ -178,6 +182,9 @@ extern "C" void NAME(collide)(const ol_lat *L, int kind, double *f, double *g, c
     case OL_NSIN_COLLIDE: NSin::MacroCollide(*p, F->rho, F->ux, F->uy, nu, save); break;
     case OL_NSIN_BRINKMAN: NSin::MacroBrinkmanCollide(*p, F->rho, F->ux, F->uy, nu, F->alpha, save); break;
     case OL_ANSIN_BRINKMAN: ANSin::MacroBrinkmanCollide(*p, F->rho, F->ux, F->uy, F->ip, F->iux, F->iuy, F->imx, F->imy, nu, F->alpha, save); break;
+    case OL_EL_COLLIDE: EL::MacroCollide(*p, F->rho, F->ux, F->uy, F->sxx, F->sxy, F->syx, F->syy, P->tau, save); break;
+    case OL_EL_EXTENDED: EL::MacroExtendedCollide(*p, F->rho, F->ux, F->uy, F->sxx, F->sxy, F->syx, F->syy, P->tau, F->gamma, save); break;
+    case OL_AEL_COLLIDE: AEL::MacroCollide(*p, F->ip, F->imx, F->imy, F->isxx, F->isxy, F->isyx, F->isyy, P->tau, F->gamma, save); break;
     }
 #else
     double gz = P->gz;
@@ -210,6 +217,8 @@ extern "C" void NAME(init)(const ol_lat *L, int which, double *f, const ol_field
     else if (which == 2) ANS::InitialCondition(*p, F->ux, F->uy, F->ip, F->iux, F->iuy);
     else if (which == 4) NSin::InitialCondition(*p, F->rho, F->ux, F->uy);
     else if (which == 5) ANSin::InitialCondition(*p, F->ux, F->uy, F->ip, F->iux, F->iuy);
+    else if (which == 6) EL::InitialCondition(*p, F->rho, F->ux, F->uy, F->sxx, F->sxy, F->syx, F->syy);
+    else if (which == 7) AEL::InitialCondition(*p, F->ip, F->imx, F->imy, F->isxx, F->isxy, F->isyx, F->isyy, F->gamma);
     else AAD::InitialCondition(*p, F->ux, F->uy, F->item, F->iqx, F->iqy);
 #else
     if (which == 0) NS::InitialCondition(*p, F->rho, F->ux, F->uy, F->uz);
@@ -230,6 +239,7 @@ extern "C" void NAME(sensitivity)(const ol_lat *L, int which, double *dfds, cons
     if (which == 0) AAD::SensitivityTemperatureAtHeatSource(*p, dfds, F->ux, F->uy, F->imx, F->imy, dads, F->tem, F->item, F->iqx, F->iqy, g, ig, F->diffusivity, dkds, QN, M);
     else if (which == 1) AAD::SensitivityBrinkmanDiffusivity(*p, dfds, F->ux, F->uy, F->imx, F->imy, dads, F->tem, F->item, F->iqx, F->iqy, g, ig, F->diffusivity, dkds);
     else if (which == 2) AAD::SensitivityHeatExchange(*p, dfds, F->ux, F->uy, F->imx, F->imy, dads, F->tem, F->item, dkds);
+    else if (which == 4) AEL::SensitivityCompliance(*p, dfds, F->sxx, F->sxy, F->syx, F->syy, F->ip, F->isxx, F->isxy, F->isyx, F->isyy);
     else ANS::SensitivityBrinkman(*p, dfds, F->ux, F->uy, F->imx, F->imy, dads);
 #else
     if (which == 0) {

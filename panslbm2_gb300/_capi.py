@@ -19,17 +19,22 @@ STORAGE = {"fp64": PL_FP64, "fp32": PL_FP32, "fp16": PL_FP16, "bf16": PL_BF16}
 NS_COLLIDE, NS_BRINKMAN, AD_NATURAL, AD_FORCE, AD_HEATEX, AD_NATURAL_NOBRINK, AD_FORCE_NOBRINK = 0, 1, 2, 3, 4, 5, 6
 NSIN_COLLIDE, NSIN_BRINKMAN = 7, 8
 ANS_BRINKMAN, AAD_NATURAL, AAD_FORCE, AAD_HEATEX, AAD_MASSFLOW, ANSIN_BRINKMAN = 10, 11, 12, 13, 14, 15
+EL_COLLIDE, EL_EXTENDED, AEL_COLLIDE = 16, 17, 18
 # boundary op kinds
 BC_WALL, BC_IWALL, BC_NS_U, BC_NS_RHO, BC_AD_T, BC_AD_Q, BC_AD_QC = 0, 1, 2, 3, 4, 5, 6
 BC_ANS_U, BC_ANS_RHO, BC_AAD_T, BC_AAD_Q, BC_AAD_RHO = 7, 8, 9, 10, 11
 BC_NSIN_U, BC_NSIN_RHO, BC_ANSIN_U = 12, 13, 14
+BC_EL_STRESS, BC_AEL_STRESS = 15, 16
 SMOOTH_CORNER, SMOOTH_AT, SMOOTH_LINE = 20, 21, 22
 # fields
-ALPHA, KAPPA, BETA, DIRX, DIRY, DIRZ = 0, 1, 2, 3, 4, 5
+ALPHA, KAPPA, BETA, DIRX, DIRY, DIRZ, DENSITY, GAMMA = 0, 1, 2, 3, 4, 5, 6, 7
 OPT_GRAPHS, OPT_SIDE_PRIORITY = 1, 2
 RHO, UX, UY, UZ, TEM, QX, QY, QZ = 8, 9, 10, 11, 12, 13, 14, 15
 IP, IUX, IUY, IUZ, IMX, IMY, IMZ, ITEM, IQX, IQY, IQZ = 16, 17, 18, 19, 20, 21, 22, 23, 24, 25, 26
 FWD_RHO, FWD_UX, FWD_UY, FWD_UZ, FWD_TEM = 32, 33, 34, 35, 36
+# the elastic kinds' macros share the planes above
+SXX, SXY, SYX, SYY = TEM, QX, QY, QZ
+IRHO, ISXX, ISXY, ISYX, ISYY = IP, ITEM, IQX, IQY, IQZ
 
 DP = C.POINTER(C.c_double)
 IPT = C.POINTER(C.c_int)
@@ -37,7 +42,7 @@ IPT = C.POINTER(C.c_int)
 
 class Phys(C.Structure):
     _fields_ = [("nu", C.c_double), ("diff", C.c_double), ("gx", C.c_double), ("gy", C.c_double),
-                ("gz", C.c_double), ("tem0", C.c_double)]
+                ("gz", C.c_double), ("tem0", C.c_double), ("tau", C.c_double)]
 
 
 class BcDesc(C.Structure):
@@ -51,9 +56,9 @@ EXPORTS = [
     "pl_create", "pl_destroy", "pl_last_error", "pl_synchronize", "pl_set_stream", "pl_set_option",
     "pl_set_shift",
     "pl_set_populations", "pl_get_populations", "pl_set_field", "pl_get_field", "pl_freeze_forward",
-    "pl_program_create", "pl_program_destroy", "pl_init", "pl_collide", "pl_step", "pl_steps", "pl_stream",
+    "pl_program_create", "pl_program_destroy", "pl_init", "pl_init_elastic", "pl_collide", "pl_step", "pl_steps", "pl_stream",
     "pl_solve", "pl_snapshot", "pl_set_snapshot", "pl_residual", "pl_residual_host", "pl_residual_device_noalloc",
-    "pl_sensitivity", "pl_heaviside_var",
+    "pl_sensitivity", "pl_sensitivity_compliance", "pl_heaviside_var",
     "pl_heaviside_sens", "pl_density_filter", "pl_normalize", "pl_stats", "pl_mma_create", "pl_mma_set_param",
     "pl_mma_update", "pl_mma_destroy", "pl_mma_get_state", "pl_mma_set_state",
 ]

@@ -83,7 +83,8 @@ struct pl_lattice_s {
     int cur = 0;
     double shift_f = 1.0, shift_g = 0.0;
     double *fld[48] = {nullptr};     // double fields by PL_* id (design inputs, forward solution)
-    void *cfld[11] = {nullptr};      // compute-type copies: alpha,kappa,beta,dirx,diry,dirz,frho,fux,fuy,fuz,ftem
+    void *cfld[13] = {nullptr};      // compute-type copies: alpha,kappa,beta,dirx,diry,dirz,frho,fux,fuy,fuz,ftem,
+                                     // EL density, gamma
     double *fwd[2][8] = {{nullptr}};
     double *adj[2][11] = {{nullptr}};
     int fwd_next = 0, adj_next = 0;  // slot the next collide writes
@@ -153,16 +154,18 @@ int check_launch(pl_lattice h, int nk) {
     h->launches += nk;
     return PL_OK;
 }
-bool valid_kind(int k) { return (k >= 0 && k <= 8) || (k >= 10 && k <= 15); }
+bool valid_kind(int k) { return (k >= 0 && k <= 8) || (k >= 10 && k <= 18); }
 // NSin / ANSin exist for D2Q9 only (nsincompressible.h, adjointnsincompressible.h)
 int check_kind(pl_lattice h, int kind) {
     if (!valid_kind(kind)) return fail(PL_ERR_ARG, "unknown collide kind %d", kind);
-    if (pl::kind_incompressible(kind) && h->nd != 2) return fail(PL_ERR_UNSUPPORTED, "kind %d is D2Q9 only", kind);
+    if ((pl::kind_incompressible(kind) || pl::kind_elastic(kind)) && h->nd != 2)
+        return fail(PL_ERR_UNSUPPORTED, "kind %d is D2Q9 only", kind);
     return PL_OK;
 }
 int field_index_c(int f) {
     if (f >= PL_ALPHA && f <= PL_DIRZ) return f;
     if (f >= PL_FWD_RHO && f <= PL_FWD_TEM) return 6 + (f - PL_FWD_RHO);
+    if (f == PL_DENSITY || f == PL_GAMMA) return 11 + (f - PL_DENSITY);
     return -1;
 }
 // make sure a compute-type copy of field f exists and is current
@@ -260,7 +263,7 @@ int compile_program(pl_lattice h, const pl_bc_desc *descs, int ndesc, Program &P
         }
         if (d.kind == PL_SMOOTH_AT) { smooth_at(d.lat, d.i, d.j, d.k, d.di, d.dj, d.dk); ++seq; continue; }
         if (d.kind == PL_SMOOTH_LINE) { smooth_line(d.lat, d.axis, d.i, d.j, d.di, d.dj); ++seq; continue; }
-        if (d.kind < PL_BC_WALL || d.kind > PL_BC_ANSIN_U)
+        if (d.kind < PL_BC_WALL || d.kind > PL_BC_AEL_STRESS)
             return fail(PL_ERR_ARG, "program desc %d: unknown kind %d", di, d.kind);
         if (d.kind >= PL_BC_NSIN_U && h->nd != 2)
             return fail(PL_ERR_UNSUPPORTED, "program desc %d: kind %d is D2Q9 only", di, d.kind);
@@ -532,17 +535,31 @@ int build_args(pl_lattice h, int kind, const pl_phys *ph, int prog, int src, int
     a.ph.nu = ph ? ph->nu : 0.0; a.ph.diff = ph ? ph->diff : 0.0;
     a.ph.gx = ph ? ph->gx : 0.0; a.ph.gy = ph ? ph->gy : 0.0; a.ph.gz = ph ? ph->gz : 0.0;
     a.ph.tem0 = ph ? ph->tem0 : 0.0;
+    a.ph.tau = ph ? ph->tau : 0.0;
     a.ph.shift_f = h->shift_f; a.ph.shift_g = h->shift_g;
     a.pull = pull ? 1 : 0;
     a.save = save ? 1 : 0;
     a.err = h->err;
     const bool adjk = pl::kind_is_adjoint(kind);
+    const bool elk = pl::kind_elastic(kind);
     a.sgn = adjk ? 1 : -1;
     // inputs required by the kind
     int r;
     if (!kind_inputs) goto program;
+    if (elk) {
+        if (kind != PL_AEL_COLLIDE) {
+            if (!h->fld[PL_DENSITY]) return fail(PL_ERR_STATE, "kind %d needs PL_DENSITY", kind);
+            if ((r = ensure_cfield(h, PL_DENSITY))) return r;
+            a.elrho = h->cfld[11];
+        }
+        if (kind != PL_EL_COLLIDE) {
+            if (!h->fld[PL_GAMMA]) return fail(PL_ERR_STATE, "kind %d needs PL_GAMMA", kind);
+            if ((r = ensure_cfield(h, PL_GAMMA))) return r;
+            a.gamma = h->cfld[12];
+        }
+    }
     if (kind == PL_NS_BRINKMAN || kind == PL_NSIN_BRINKMAN || kind == PL_AD_NATURAL || kind == PL_AD_FORCE ||
-        kind == PL_AD_HEATEX || adjk) {
+        kind == PL_AD_HEATEX || (adjk && !elk)) {
         if (!h->fld[PL_ALPHA]) return fail(PL_ERR_STATE, "kind %d needs PL_ALPHA", kind);
         if ((r = ensure_cfield(h, PL_ALPHA))) return r;
         a.alpha = h->cfld[0];
@@ -564,7 +581,7 @@ int build_args(pl_lattice h, int kind, const pl_phys *ph, int prog, int src, int
         }
         a.dirx = h->cfld[3]; a.diry = h->cfld[4]; a.dirz = h->cfld[5];
     }
-    if (adjk) {
+    if (adjk && !elk) {
         for (int f = PL_FWD_RHO; f <= PL_FWD_TEM; ++f) {
             if (f == PL_FWD_UZ && h->nd == 2) continue;
             if (f == PL_FWD_TEM && (kind == PL_ANS_BRINKMAN || kind == PL_ANSIN_BRINKMAN)) continue;
@@ -911,7 +928,7 @@ int pl_get_populations(pl_lattice h, int set, double *host) {
 int pl_set_field(pl_lattice h, int f, const double *host) {
     if (!h || !host) return fail(PL_ERR_ARG, "bad arguments");
     int r;
-    if ((f >= PL_ALPHA && f <= PL_DIRZ) || (f >= PL_FWD_RHO && f <= PL_FWD_TEM)) {
+    if ((f >= PL_ALPHA && f <= PL_GAMMA) || (f >= PL_FWD_RHO && f <= PL_FWD_TEM)) {
         if ((r = ensure_d(h, &h->fld[f], h->n))) return r;
         if ((r = upload(h, h->fld[f], host, h->n))) return r;
         return sync_cfield(h, f);
@@ -934,7 +951,7 @@ int pl_set_field(pl_lattice h, int f, const double *host) {
 int pl_get_field(pl_lattice h, int f, double *host) {
     if (!h || !host) return fail(PL_ERR_ARG, "bad arguments");
     const double *src = nullptr;
-    if ((f >= PL_ALPHA && f <= PL_DIRZ) || (f >= PL_FWD_RHO && f <= PL_FWD_TEM)) src = h->fld[f];
+    if ((f >= PL_ALPHA && f <= PL_GAMMA) || (f >= PL_FWD_RHO && f <= PL_FWD_TEM)) src = h->fld[f];
     else if (f >= PL_RHO && f <= PL_QZ) src = h->fwd_saved >= 0 ? h->fwd[h->fwd_saved][f - PL_RHO] : nullptr;
     else if (f >= PL_IP && f <= PL_IQZ) src = h->adj_saved >= 0 ? h->adj[h->adj_saved][f - PL_IP] : nullptr;
     else return fail(PL_ERR_ARG, "unknown field %d", f);
@@ -1002,6 +1019,36 @@ int pl_init(pl_lattice h, int which, const double *a0, const double *a1, const d
     a.geo.n = h->n; a.geo.np = h->np; a.dst = h->pop[h->cur];
     a.ph.shift_f = h->shift_f; a.ph.shift_g = h->shift_g;
     h->aux(pl::AUX_INIT, a, which, in, 0, 0, nullptr, 0, 0.0, h->st);
+    if ((r = check_launch(h, 1))) return r;
+    return pl_synchronize(h);
+}
+
+int pl_init_elastic(pl_lattice h, int which, const double *const *in) {
+    if (!h || !in || (which != 0 && which != 1)) return fail(PL_ERR_ARG, "bad arguments");
+    if (h->nd != 2) return fail(PL_ERR_UNSUPPORTED, "the elastic initial conditions are D2Q9 only");
+    for (int m = 0; m < 7; ++m)
+        if (!in[m]) return fail(PL_ERR_ARG, "elastic init needs seven arrays (array %d is NULL)", m);
+    int r;
+    KArgs a;
+    memset(&a, 0, sizeof a);
+    if (which == 1) {
+        if (!h->fld[PL_GAMMA]) return fail(PL_ERR_STATE, "AEL init needs PL_GAMMA");
+        if ((r = ensure_cfield(h, PL_GAMMA))) return r;
+        a.gamma = h->cfld[12];
+    }
+    double *buf;
+    if ((r = scratch(h, 1, &buf))) return r;   // q*N doubles >= 7*N
+    // kernel slots (in0, in1, in2, in3, ux, uy, uz) <- (rho | irho, s.., u | im, s..)
+    static const int slot_of_input[7] = {0, 4, 5, 1, 2, 3, 6};
+    const double *dev[7];
+    for (int m = 0; m < 7; ++m) {
+        double *d = buf + (size_t)slot_of_input[m] * h->n;
+        if ((r = upload(h, d, in[m], h->n))) return r;
+        dev[slot_of_input[m]] = d;
+    }
+    a.geo.n = h->n; a.geo.np = h->np; a.dst = h->pop[h->cur];
+    a.ph.shift_f = h->shift_f; a.ph.shift_g = h->shift_g;
+    h->aux(pl::AUX_INIT, a, 6 + which, dev, 0, 0, nullptr, 0, 0.0, h->st);
     if ((r = check_launch(h, 1))) return r;
     return pl_synchronize(h);
 }
@@ -1256,6 +1303,38 @@ int pl_sensitivity(pl_lattice h, int which, double *dfds, const double *dads, co
     pl::launch_sensitivity(h->q, s, h->st);
     if ((r = check_launch(h, 1))) return r;
     return download(h, dfds, d_dfds, h->n);
+}
+
+int pl_sensitivity_compliance(pl_lattice h, double *dfds, const double *const *in) {
+    if (!h || !dfds) return fail(PL_ERR_ARG, "bad arguments");
+    if (h->nd != 2) return fail(PL_ERR_UNSUPPORTED, "the compliance sensitivity is D2Q9 only");
+    double *buf;
+    int r = scratch(h, 4, &buf);   // q*N = 9*N: dfds + up to 8 inputs; the ninth in scratch 5
+    if (r) return r;
+    double *sc5;
+    if ((r = scratch(h, 5, &sc5))) return r;
+    const double *dev[9];
+    if (in) {
+        for (int m = 0; m < 9; ++m) {
+            if (!in[m]) return fail(PL_ERR_ARG, "compliance sensitivity input %d is NULL", m);
+            double *d = m < 8 ? buf + (size_t)(m + 1) * h->n : sc5;
+            if ((r = upload(h, d, in[m], h->n))) return r;
+            dev[m] = d;
+        }
+    } else {
+        // the stress of the last saving EL collide and the adjoint of the last saving AEL collide
+        if (h->fwd_saved < 0 || h->adj_saved < 0) return fail(PL_ERR_STATE, "no saved EL / AEL collide");
+        const int fs = h->fwd_saved, as = h->adj_saved;
+        static const int adj_plane[5] = {0, 7, 8, 9, 10};
+        for (int m = 0; m < 4; ++m) dev[m] = h->fwd[fs][4 + m];
+        for (int m = 0; m < 5; ++m) dev[4 + m] = h->adj[as][adj_plane[m]];
+        for (int m = 0; m < 9; ++m)
+            if (!dev[m]) return fail(PL_ERR_STATE, "saved EL / AEL macros missing");
+    }
+    if ((r = upload(h, buf, dfds, h->n))) return r;
+    pl::launch_compliance(h->n, buf, dev, h->st);
+    if ((r = check_launch(h, 1))) return r;
+    return download(h, dfds, buf, h->n);
 }
 
 static int filter_common(pl_lattice h, int op, double R, double beta, const double *s, const double *d,

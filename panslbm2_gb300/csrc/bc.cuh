@@ -361,6 +361,62 @@ __device__ __forceinline__ void apply_op(const Op &op, T *f, T *g, int node, con
         }
         break;
     } break;
+    case BC_EL_STRESS:
+    case BC_AEL_STRESS: if constexpr (!SIMPLE && ND == 2 && Q == 9) {
+        // EL::BoundaryConditionSetStressAlong{X,Y}Edge (elastic.h:60-104): the three incoming
+        // populations from the node's known ones and the traction (tx, ty);
+        // AEL::iBoundaryConditionSetStressAlong{X,Y}Edge (adjointelastic.h:48-92): the three
+        // outgoing adjoint populations, traction over the node's density (v2). D2Q9 indices.
+        T *p = f;
+        const T tx = T(op.v0), ty = T(op.v1);
+        if (op.kind == BC_EL_STRESS) {
+            if (A == 0 && d < 0) {
+                const T s = p[3] + p[6] + p[7];
+                p[1] = p[3] - T(4) * s / T(3) + T(2) * tx / T(3);
+                p[5] = p[6] - s / T(3) + (tx + T(3) * ty) / T(6);
+                p[8] = p[7] - s / T(3) + (tx - T(3) * ty) / T(6);
+            } else if (A == 0) {
+                const T s = p[1] + p[5] + p[8];
+                p[3] = p[1] - T(4) * s / T(3) - T(2) * tx / T(3);
+                p[6] = p[5] - s / T(3) - (tx - T(3) * ty) / T(6);
+                p[7] = p[8] - s / T(3) - (tx + T(3) * ty) / T(6);
+            } else if (d < 0) {
+                const T s = p[4] + p[7] + p[8];
+                p[2] = p[4] - T(4) * s / T(3) + T(2) * ty / T(3);
+                p[5] = p[8] - s / T(3) + (ty + T(3) * tx) / T(6);
+                p[6] = p[7] - s / T(3) + (ty - T(3) * tx) / T(6);
+            } else {
+                const T s = p[2] + p[5] + p[6];
+                p[4] = p[2] - T(4) * s / T(3) - T(2) * ty / T(3);
+                p[7] = p[6] - s / T(3) - (ty + T(3) * tx) / T(6);
+                p[8] = p[5] - s / T(3) - (ty - T(3) * tx) / T(6);
+            }
+        } else {
+            const T rho = T(op.v2);
+            if (A == 0 && d < 0) {
+                const T s = (T(4) * p[1] + p[5] + p[8]) / T(3);
+                p[3] = p[1] - s + T(2) * tx / rho;
+                p[6] = p[5] - s + T(2) * (tx - ty) / rho;
+                p[7] = p[8] - s + T(2) * (tx + ty) / rho;
+            } else if (A == 0) {
+                const T s = (T(4) * p[3] + p[6] + p[7]) / T(3);
+                p[1] = p[3] - s - T(2) * tx / rho;
+                p[5] = p[6] - s - T(2) * (tx + ty) / rho;
+                p[8] = p[7] - s - T(2) * (tx - ty) / rho;
+            } else if (d < 0) {
+                const T s = (T(4) * p[2] + p[5] + p[6]) / T(3);
+                p[4] = p[2] - s + T(2) * ty / rho;
+                p[7] = p[6] - s + T(2) * (ty + tx) / rho;
+                p[8] = p[5] - s + T(2) * (ty - tx) / rho;
+            } else {
+                const T s = (T(4) * p[4] + p[7] + p[8]) / T(3);
+                p[2] = p[4] - s - T(2) * ty / rho;
+                p[5] = p[8] - s - T(2) * (ty + tx) / rho;
+                p[6] = p[7] - s - T(2) * (ty - tx) / rho;
+            }
+        }
+        break;
+    } break;
     default:
         break;
     }

@@ -9,15 +9,20 @@ enum Kind {
     K_NS_COLLIDE = 0, K_NS_BRINKMAN = 1, K_AD_NATURAL = 2, K_AD_FORCE = 3, K_AD_HEATEX = 4,
     K_AD_NATURAL_NOBRINK = 5, K_AD_FORCE_NOBRINK = 6, K_NSIN_COLLIDE = 7, K_NSIN_BRINKMAN = 8,
     K_ANS_BRINKMAN = 10, K_AAD_NATURAL = 11, K_AAD_FORCE = 12, K_AAD_HEATEX = 13, K_AAD_MASSFLOW = 14,
-    K_ANSIN_BRINKMAN = 15
+    K_ANSIN_BRINKMAN = 15, K_EL_COLLIDE = 16, K_EL_EXTENDED = 17, K_AEL_COLLIDE = 18
 };
-__host__ __device__ constexpr bool kind_is_adjoint(int k) { return k >= 10; }
+__host__ __device__ constexpr bool kind_is_adjoint(int k) { return (k >= 10 && k <= 15) || k == K_AEL_COLLIDE; }
+// the elastic variants (EL / AEL), defined by the reference for D2Q9 only
+__host__ __device__ constexpr bool kind_elastic(int k) {
+    return k == K_EL_COLLIDE || k == K_EL_EXTENDED || k == K_AEL_COLLIDE;
+}
 // the incompressible variants (NSin / ANSin), defined by the reference for D2Q9 only
 __host__ __device__ constexpr bool kind_incompressible(int k) {
     return k == K_NSIN_COLLIDE || k == K_NSIN_BRINKMAN || k == K_ANSIN_BRINKMAN;
 }
 __host__ __device__ constexpr bool kind_has_g(int k) {
-    return !(k == K_NS_COLLIDE || k == K_NS_BRINKMAN || k == K_ANS_BRINKMAN || kind_incompressible(k));
+    return !(k == K_NS_COLLIDE || k == K_NS_BRINKMAN || k == K_ANS_BRINKMAN || kind_incompressible(k) ||
+             kind_elastic(k));
 }
 __host__ __device__ constexpr bool kind_node_kappa(int k) {
     return k == K_AD_NATURAL || k == K_AD_FORCE || k == K_AAD_NATURAL || k == K_AAD_FORCE || k == K_AAD_MASSFLOW;
@@ -35,6 +40,7 @@ enum BcKind {
     BC_WALL = 0, BC_IWALL = 1, BC_NS_U = 2, BC_NS_RHO = 3, BC_AD_T = 4, BC_AD_Q = 5, BC_AD_QC = 6,
     BC_ANS_U = 7, BC_ANS_RHO = 8, BC_AAD_T = 9, BC_AAD_Q = 10, BC_AAD_RHO = 11,
     BC_NSIN_U = 12, BC_NSIN_RHO = 13, BC_ANSIN_U = 14,   // D2Q9 only
+    BC_EL_STRESS = 15, BC_AEL_STRESS = 16,               // D2Q9 only
     BC_SMOOTH = 20
 };
 
@@ -92,7 +98,7 @@ struct Geo {
     const uint8_t *flags; // optional per-node "has boundary ops" flags (interior lines)
 };
 
-struct Phys { double nu, diff, gx, gy, gz, tem0, shift_f, shift_g; };
+struct Phys { double nu, diff, gx, gy, gz, tem0, shift_f, shift_g, tau; };
 
 // Arguments of every population kernel. Field pointers are device pointers; `T*` members are
 // stored as void* and cast to the kernel's compute type.
@@ -102,8 +108,11 @@ struct KArgs {
     void *dst;                  // populations written
     const void *alpha, *kappa, *beta, *dirx, *diry, *dirz;   // design fields, compute type
     const void *fwd[5];         // adjoint kinds: forward rho, ux, uy, uz, tem (compute type)
+    const void *elrho, *gamma;  // elastic kinds: density and stress scale (compute type)
     double *out[11];            // macro outputs (forward: rho,ux,uy,uz,tem,qx,qy,qz;
-                                //  adjoint: ip,iux,iuy,iuz,imx,imy,imz,item,iqx,iqy,iqz)
+                                //  adjoint: ip,iux,iuy,iuz,imx,imy,imz,item,iqx,iqy,iqz;
+                                //  EL: ux,uy in 1,2 and sxx,sxy,syx,syy in 4..7;
+                                //  AEL: irho 0, imx,imy 4,5, isxx,isxy,isyx,isyy 7..10)
     double *snap;               // pre-collision g snapshot, [q][np] planes
     // boundary program
     const int *bnode;           // boundary nodes (sorted)

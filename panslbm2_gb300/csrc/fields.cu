@@ -179,6 +179,26 @@ void launch_sensitivity(int q, const SensArgs &s, cudaStream_t st) {
     else k_sens<D3Q15><<<g, kRB, 0, st>>>(s);
 }
 
+// AEL::SensitivityCompliance (adjointelastic.h:149-155), in the reference's expression order with
+// every product and sum rounded on its own (no contraction), so it matches the CPU bit for bit
+struct CompArgs { const double *in[9]; };
+__global__ void k_compliance(int n, double *dfds, CompArgs c) {
+    const int i = blockIdx.x * kRB + threadIdx.x;
+    if (i >= n) return;
+    const double sxx = c.in[0][i], sxy = c.in[1][i], syx = c.in[2][i], syy = c.in[3][i];
+    double ss = __dmul_rn(sxx, c.in[5][i]);
+    ss = __dadd_rn(ss, __dmul_rn(sxy, c.in[6][i]));
+    ss = __dadd_rn(ss, __dmul_rn(syx, c.in[7][i]));
+    ss = __dadd_rn(ss, __dmul_rn(syy, c.in[8][i]));
+    const double tr = __dmul_rn(__dmul_rn(1.5, c.in[4][i]), __dadd_rn(sxx, syy));
+    dfds[i] = __dadd_rn(dfds[i], __dsub_rn(__dmul_rn(4.5, ss), tr));
+}
+void launch_compliance(int n, double *dfds, const double *const *in, cudaStream_t st) {
+    CompArgs c;
+    for (int m = 0; m < 9; ++m) c.in[m] = in[m];
+    k_compliance<<<(n + kRB - 1) / kRB, kRB, 0, st>>>(n, dfds, c);
+}
+
 // ---- filters ------------------------------------------------------------------------------
 // Taps of the (2 nR + 1)^d box with distance <= R, in the reference's (i2, j2, k2) loop order,
 // with their hat weights (R - dist)/R computed on the host in FP64.

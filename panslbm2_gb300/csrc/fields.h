@@ -27,6 +27,9 @@ struct SensArgs {
     const double *g, *ig;                           // snapshots, [q][np]
 };
 void launch_sensitivity(int q, const SensArgs &s, cudaStream_t st);
+// AEL::SensitivityCompliance: dfds[i] += 4.5 s:is - 1.5 irho tr s; in = sxx, sxy, syx, syy, irho,
+// isxx, isxy, isyx, isyy (device arrays of n)
+void launch_compliance(int n, double *dfds, const double *const *in, cudaStream_t st);
 
 struct FiltArgs {
     int n, nx, ny, nz, ntap;

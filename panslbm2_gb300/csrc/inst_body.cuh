@@ -1,7 +1,7 @@
 // inst_body.cuh -- explicit kernel instantiations and launch switch for one
 // (lattice, storage) pair. Included by inst_<lattice>_<storage>.cu with PL_LAT, PL_STORE and
 // PL_NAME defined; PL_ALL_KINDS selects every collide kind (else the primary ones only) and
-// PL_INCOMPRESSIBLE adds the D2Q9-only NSin / ANSin kinds.
+// PL_INCOMPRESSIBLE adds the D2Q9-only NSin / ANSin kinds, PL_ELASTIC the D2Q9-only EL / AEL kinds.
 #include "kernels.cuh"
 #include "launch.h"
 
@@ -33,6 +33,11 @@ static __device__ __forceinline__ void collide_any(int kind, TC *f, TC *g, int i
     case K_NSIN_COLLIDE: collide_node<PL_LAT, TC, K_NSIN_COLLIDE>(f, g, idx, a, save, nullptr, a.geo.np, u); break;
     case K_NSIN_BRINKMAN: collide_node<PL_LAT, TC, K_NSIN_BRINKMAN>(f, g, idx, a, save, nullptr, a.geo.np, u); break;
     case K_ANSIN_BRINKMAN: collide_node<PL_LAT, TC, K_ANSIN_BRINKMAN>(f, g, idx, a, save, nullptr, a.geo.np, nullptr); break;
+#endif
+#if defined(PL_ALL_KINDS) && defined(PL_ELASTIC)
+    case K_EL_COLLIDE: collide_node<PL_LAT, TC, K_EL_COLLIDE>(f, g, idx, a, save, nullptr, a.geo.np, u); break;
+    case K_EL_EXTENDED: collide_node<PL_LAT, TC, K_EL_EXTENDED>(f, g, idx, a, save, nullptr, a.geo.np, u); break;
+    case K_AEL_COLLIDE: collide_node<PL_LAT, TC, K_AEL_COLLIDE>(f, g, idx, a, save, nullptr, a.geo.np, nullptr); break;
 #endif
     default: break;
     }
@@ -167,6 +172,11 @@ int PL_CAT(launch_, PL_NAME)(int kind, int op, bool save, const KArgs &a, cudaSt
     case K_NSIN_COLLIDE: run_kind<K_NSIN_COLLIDE>(op, save, a, st); return 0;
     case K_NSIN_BRINKMAN: run_kind<K_NSIN_BRINKMAN>(op, save, a, st); return 0;
     case K_ANSIN_BRINKMAN: run_kind<K_ANSIN_BRINKMAN>(op, save, a, st); return 0;
+#endif
+#if defined(PL_ALL_KINDS) && defined(PL_ELASTIC)
+    case K_EL_COLLIDE: run_kind<K_EL_COLLIDE>(op, save, a, st); return 0;
+    case K_EL_EXTENDED: run_kind<K_EL_EXTENDED>(op, save, a, st); return 0;
+    case K_AEL_COLLIDE: run_kind<K_AEL_COLLIDE>(op, save, a, st); return 0;
 #endif
     default: return -1;
     }

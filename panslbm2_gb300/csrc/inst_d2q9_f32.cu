@@ -4,4 +4,5 @@
 #define PL_NAME d2q9_f32
 #define PL_ALL_KINDS
 #define PL_INCOMPRESSIBLE
+#define PL_ELASTIC
 #include "inst_body.cuh"

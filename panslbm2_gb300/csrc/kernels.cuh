@@ -100,8 +100,8 @@ __device__ __forceinline__ void node_tail(const KArgs &a, int idx, int code, typ
         }
     }
     T u[3];
-    collide_node<L, T, K>(f, g, idx, a, a.save != 0, nullptr, a.geo.np, (INL && K < 10) ? u : nullptr);
-    if constexpr (INL && K < 10) {
+    collide_node<L, T, K>(f, g, idx, a, a.save != 0, nullptr, a.geo.np, (INL && !kind_is_adjoint(K)) ? u : nullptr);
+    if constexpr (INL && !kind_is_adjoint(K)) {
         if (code >= 0 && a.bcu_out[0]) {
             a.bcu_out[0][idx] = double(u[0]);
             a.bcu_out[1][idx] = double(u[1]);
@@ -137,7 +137,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_interior(KArgs a) {
     }
     T f[L::Q], g[L::Q];
     const T sf = T(a.ph.shift_f), sg = T(a.ph.shift_g);
-    load_node<L, S, HG>(static_cast<const S *>(a.src), a.geo, idx, i, j, k, PULL, K >= 10 ? 1 : -1,
+    load_node<L, S, HG>(static_cast<const S *>(a.src), a.geo, idx, i, j, k, PULL, kind_is_adjoint(K) ? 1 : -1,
                         is_interior<L>(a.geo, i, j, k), f, g, sf, sg);
     node_tail<L, S, K>(a, idx, PULL ? code : -1, f, g, sf, sg);
 }
@@ -194,10 +194,10 @@ __global__ void __launch_bounds__(128) k_boundary(KArgs a) {
     if (s >= a.nb) return;
     const int idx = a.bnode[s];
     T f[L::Q], g[L::Q];
-    eval_node<L, S, 4>(a, idx, 0x7fffffff, f, g, HG, K >= 10 ? 1 : -1);
+    eval_node<L, S, 4>(a, idx, 0x7fffffff, f, g, HG, kind_is_adjoint(K) ? 1 : -1);
     T u[3];
-    collide_node<L, T, K>(f, g, idx, a, a.save != 0, nullptr, a.geo.np, K < 10 ? u : nullptr);
-    if (K < 10 && a.bcu_out[0]) {
+    collide_node<L, T, K>(f, g, idx, a, a.save != 0, nullptr, a.geo.np, !kind_is_adjoint(K) ? u : nullptr);
+    if (!kind_is_adjoint(K) && a.bcu_out[0]) {
         a.bcu_out[0][idx] = double(u[0]);
         a.bcu_out[1][idx] = double(u[1]);
         if (L::ND == 3) a.bcu_out[2][idx] = double(u[2]);
@@ -255,7 +255,7 @@ __global__ void __launch_bounds__(128) k_snapshot(KArgs a) {
     const int idx = blockIdx.x * 128 + threadIdx.x;
     if (idx >= a.geo.n) return;
     T f[L::Q], g[L::Q];
-    eval_node<L, S, 4>(a, idx, 0x7fffffff, f, g, true, K >= 10 ? 1 : -1);
+    eval_node<L, S, 4>(a, idx, 0x7fffffff, f, g, true, kind_is_adjoint(K) ? 1 : -1);
     collide_node<L, T, K>(f, g, idx, a, false, a.snap, a.geo.np, nullptr);
 }
 
@@ -275,7 +275,9 @@ __global__ void __launch_bounds__(128) k_stream_program(KArgs a, int has_g, int 
 // ---- equilibrium initial conditions (navierstokes.h:548-572, advection.h:1046-1070,
 //      adjointnavierstokes.h:472-498, adjointadvection.h:1357-1381) ---------------------------
 // which: 0 NS (rho,u), 1 AD (T,u), 2 ANS (ip,iu; u), 3 AAD (iT,iq; u), 4 NSin (rho,u),
-// 5 ANSin (ip,iu) (nsincompressible.h:202-212, adjointnsincompressible.h:180-192). in[]: double
+// 5 ANSin (ip,iu) (nsincompressible.h:202-212, adjointnsincompressible.h:180-192), 6 EL (in0 rho,
+// u, in1..in3 + uz = sxx, sxy, syx, syy; elastic.h:168-179), 7 AEL (in0 irho, u = imx, imy,
+// in1..in3 + uz = isxx, isxy, isyx, isyy, gamma field; adjointelastic.h:127-138). in[]: double
 // fields.
 template <class L, class S>
 __global__ void k_init(KArgs a, int which, const double *in0, const double *in1, const double *in2,
@@ -284,7 +286,7 @@ __global__ void k_init(KArgs a, int which, const double *in0, const double *in1,
     const int idx = blockIdx.x * kBlock + threadIdx.x;
     if (idx >= a.geo.n) return;
     constexpr int Q = L::Q;
-    const T u[3] = {T(ux[idx]), T(uy[idx]), L::ND == 3 ? T(uz[idx]) : T(0)};
+    const T u[3] = {T(ux[idx]), T(uy[idx]), (L::ND == 3 && which < 6) ? T(uz[idx]) : T(0)};
     S *dst = static_cast<S *>(a.dst);
     const int set = (which == 1 || which == 3) ? 1 : 0;
     const T sh = set ? T(a.ph.shift_g) : T(a.ph.shift_f);
@@ -308,6 +310,15 @@ __global__ void k_init(KArgs a, int which, const double *in0, const double *in1,
         const T iu[3] = {T(in1[idx]), T(in2[idx]), T(0)};
 #pragma unroll
         for (int c = 0; c < Q; ++c) eq[c] = ansin_feq<L, T>(c, T(in0[idx]), iu);
+    } else if (which == 6) {
+        const T sg[4] = {T(in1[idx]), T(in2[idx]), T(in3[idx]), T(uz[idx])};
+#pragma unroll
+        for (int c = 0; c < Q; ++c) eq[c] = el_feq<L, T>(c, T(in0[idx]), u, sg);
+    } else if (which == 7) {
+        const T m[7] = {T(in0[idx]), u[0], u[1], T(in1[idx]), T(in2[idx]), T(in3[idx]), T(uz[idx])};
+        const T gm = ldT<T>(a.gamma, idx);
+#pragma unroll
+        for (int c = 0; c < Q; ++c) eq[c] = ael_feq<L, T>(c, m, gm);
     } else {
         const T iq[3] = {T(in1[idx]), T(in2[idx]), L::ND == 3 ? T(in3[idx]) : T(0)};
         const T v = T(in0[idx]) + T(3) * vdot<L, T>(u, iq);

@@ -242,6 +242,100 @@ template <class L, class T> __device__ __forceinline__ void ansin_brinkman(T *f,
 
 template <class T> __device__ __forceinline__ T ldT(const void *p, int idx) { return static_cast<const T *>(p)[idx]; }
 
+// ---- elastic LBM (EL / AEL), D2Q9 only in the reference ----------------------------------
+// EL::Macro (elastic.h:17-47): u = (sum_{c>=1} c f) / rho, s_ab = -sum_{c>=1} c_a c_b f.
+// s = {sxx, sxy, syx, syy}.
+template <class L, class T> __device__ __forceinline__ void el_macro(const T *f, T rho, T *u, T *s) {
+    T ux = T(0), uy = T(0), sxx = T(0), sxy = T(0), syx = T(0), syy = T(0);
+#pragma unroll
+    for (int c = 1; c < L::Q; ++c) {
+        const T v = f[c], cx = T(comp<L>(c, 0)), cy = T(comp<L>(c, 1));
+        ux += cx * v;
+        uy += cy * v;
+        sxx -= cx * cx * v;
+        sxy -= cx * cy * v;
+        syx -= cy * cx * v;
+        syy -= cy * cy * v;
+    }
+    const T invrho = T(1) / rho;
+    u[0] = ux * invrho; u[1] = uy * invrho; u[2] = T(0);
+    s[0] = sxx; s[1] = sxy; s[2] = syx; s[3] = syy;
+}
+// EL::Equilibrium (elastic.h:49-58): w (3 rho c.u - 4.5 c.s.c + 1.5 tr s)
+template <class L, class T> __device__ __forceinline__ T el_feq(int c, T rho, const T *u, const T *s) {
+    const T cx = T(comp<L>(c, 0)), cy = T(comp<L>(c, 1));
+    const T ciu = cx * u[0] + cy * u[1];
+    const T cisci = cx * s[0] * cx + cx * s[1] * cy + cy * s[2] * cx + cy * s[3] * cy;
+    const T trss = s[0] + s[3];
+    return wt<L, T>(c) * (T(3) * rho * ciu - T(4.5) * cisci + T(1.5) * trss);
+}
+// AEL::Macro (adjointelastic.h:16-35): m = {irho, imx, imy, isxx, isxy, isyx, isyy} with
+// irho = sum w f, im = sum w c f, is_ab = sum w c_a c_b f
+template <class L, class T> __device__ __forceinline__ void ael_macro(const T *f, T *m) {
+    T irho = wt<L, T>(0) * f[0], imx = T(0), imy = T(0), isxx = T(0), isxy = T(0), isyx = T(0), isyy = T(0);
+#pragma unroll
+    for (int c = 1; c < L::Q; ++c) {
+        const T v = f[c], e = wt<L, T>(c), cx = T(comp<L>(c, 0)), cy = T(comp<L>(c, 1));
+        irho += e * v;
+        imx += e * cx * v;
+        imy += e * cy * v;
+        isxx += e * cx * cx * v;
+        isxy += e * cx * cy * v;
+        isyx += e * cy * cx * v;
+        isyy += e * cy * cy * v;
+    }
+    m[0] = irho; m[1] = imx; m[2] = imy; m[3] = isxx; m[4] = isxy; m[5] = isyx; m[6] = isyy;
+}
+// AEL::Equilibrium (adjointelastic.h:37-46): 3 im.c + 4.5 gamma c.is.c - 1.5 gamma irho |c|^2
+template <class L, class T> __device__ __forceinline__ T ael_feq(int c, const T *m, T gamma) {
+    const int icx = comp<L>(c, 0), icy = comp<L>(c, 1);
+    const T cx = T(icx), cy = T(icy);
+    const T imc = m[1] * cx + m[2] * cy;
+    const T cisc = cx * m[3] * cx + cx * m[4] * cy + cy * m[5] * cx + cy * m[6] * cy;
+    const T irhocc = m[0] * T(icx * icx + icy * icy);
+    return T(3) * imc + T(4.5) * gamma * cisc - T(1.5) * gamma * irhocc;
+}
+
+// EL::MacroCollide / MacroExtendedCollide (elastic.h:109-166) and AEL::MacroCollide
+// (adjointelastic.h:96-125) for one node; the BGK rate is 1 / tau
+template <class L, class T, int K>
+__device__ __forceinline__ void collide_elastic(T *f, int idx, const KArgs &a, bool save, T *uout) {
+    constexpr int Q = L::Q;
+    const T om = T(1) / T(a.ph.tau), iom = T(1) - om;
+    if (K == K_EL_COLLIDE || K == K_EL_EXTENDED) {
+        const T rho = ldT<T>(a.elrho, idx);
+        T u[3], s[4];
+        el_macro<L, T>(f, rho, u, s);
+        if (K == K_EL_EXTENDED) {
+            const T gm = ldT<T>(a.gamma, idx);
+#pragma unroll
+            for (int m = 0; m < 4; ++m) s[m] *= gm;
+        }
+        if (save) {
+            if (a.out[1]) a.out[1][idx] = double(u[0]);
+            if (a.out[2]) a.out[2][idx] = double(u[1]);
+#pragma unroll
+            for (int m = 0; m < 4; ++m) if (a.out[4 + m]) a.out[4 + m][idx] = double(s[m]);
+        }
+        if (uout) { uout[0] = u[0]; uout[1] = u[1]; uout[2] = T(0); }
+#pragma unroll
+        for (int c = 0; c < Q; ++c) f[c] = iom * f[c] + om * el_feq<L, T>(c, rho, u, s);
+    } else {
+        T m[7];
+        ael_macro<L, T>(f, m);
+        if (save) {
+            if (a.out[0]) a.out[0][idx] = double(m[0]);
+            if (a.out[4]) a.out[4][idx] = double(m[1]);
+            if (a.out[5]) a.out[5][idx] = double(m[2]);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) if (a.out[7 + k]) a.out[7 + k][idx] = double(m[3 + k]);
+        }
+        const T gm = ldT<T>(a.gamma, idx);
+#pragma unroll
+        for (int c = 0; c < Q; ++c) f[c] = iom * f[c] + om * ael_feq<L, T>(c, m, gm);
+    }
+}
+
 // NSin::MacroCollide / MacroBrinkmanCollide (nsincompressible.h:144-200) and
 // ANSin::MacroBrinkmanCollide (adjointnsincompressible.h:143-178) for one node
 template <class L, class T, int K>
@@ -298,6 +392,10 @@ __device__ __forceinline__ void collide_node(T *f, T *g, int idx, const KArgs &a
         collide_incompressible<L, T, K>(f, idx, a, save, uout);
         return;
     }
+    if constexpr (kind_elastic(K)) {
+        collide_elastic<L, T, K>(f, idx, a, save, uout);
+        return;
+    }
     constexpr int Q = L::Q;
     const T omf = T(1) / (T(3) * T(a.ph.nu) + T(0.5));
     T omg = T(0);
@@ -306,7 +404,7 @@ __device__ __forceinline__ void collide_node(T *f, T *g, int idx, const KArgs &a
     else if (kind_has_g(K))
         omg = T(1) / (T(3) * T(a.ph.diff) + T(0.5));
     const T gv[3] = {T(a.ph.gx), T(a.ph.gy), T(a.ph.gz)};
-    if (K < 10) {
+    if (!kind_is_adjoint(K)) {
         T rho, u[3], tem = T(0), q[3] = {T(0), T(0), T(0)};
         ns_macro<L, T>(f, rho, u);
         if (kind_has_g(K)) ad_macro<L, T>(g, u, omg, tem, q);

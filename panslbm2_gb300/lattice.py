@@ -34,8 +34,8 @@ def _i32(a, n=None):
     return a
 
 
-def phys(nu=0.1, diff=0.0, gx=0.0, gy=0.0, gz=0.0, tem0=0.0):
-    return A.Phys(nu, diff, gx, gy, gz, tem0)
+def phys(nu=0.1, diff=0.0, gx=0.0, gy=0.0, gz=0.0, tem0=0.0, tau=0.0):
+    return A.Phys(nu, diff, gx, gy, gz, tem0, tau)
 
 
 class Desc:
@@ -146,6 +146,28 @@ class LatticePair:
     def init(self, which, a0, a1=None, a2=None, a3=None, ux=None, uy=None, uz=None):
         arrs = [_f64(x, self.n) for x in (a0, a1, a2, a3, ux, uy, uz)]
         check(self.lib.pl_init(self.h, which, *[_dp(x) for x in arrs]))
+
+    def init_elastic(self, which, arrays):
+        """EL (which 0: rho, ux, uy, sxx, sxy, syx, syy) or AEL (which 1: irho, imx, imy, isxx, isxy,
+        isyx, isyy; gamma from the GAMMA field) initial condition."""
+        arrs = [_f64(x, self.n) for x in arrays]
+        if len(arrs) != 7:
+            raise ValueError("seven arrays expected")
+        P = (A.DP * 7)(*[_dp(x) for x in arrs])
+        check(self.lib.pl_init_elastic(self.h, which, P))
+
+    def sensitivity_compliance(self, dfds, arrays=None):
+        """AEL::SensitivityCompliance: dfds + 4.5 s:is - 1.5 irho tr s over (sxx, sxy, syx, syy, irho,
+        isxx, isxy, isyx, isyy), or over the last saved EL / AEL macros when arrays is None."""
+        dfds = _f64(dfds, self.n).copy()
+        P = None
+        if arrays is not None:
+            arrs = [_f64(x, self.n) for x in arrays]
+            if len(arrs) != 9:
+                raise ValueError("nine arrays expected")
+            P = (A.DP * 9)(*[_dp(x) for x in arrs])
+        check(self.lib.pl_sensitivity_compliance(self.h, _dp(dfds), P))
+        return dfds
 
     def collide(self, kind, ph, save=True):
         check(self.lib.pl_collide(self.h, kind, C.byref(ph), int(save)))

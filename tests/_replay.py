@@ -3,7 +3,8 @@ import numpy as np
 
 from panslbm2_gb300 import _capi as A
 
-F_KINDS = (A.BC_NS_U, A.BC_NS_RHO, A.BC_ANS_U, A.BC_ANS_RHO, A.BC_AAD_RHO, A.BC_NSIN_U, A.BC_NSIN_RHO, A.BC_ANSIN_U)
+F_KINDS = (A.BC_NS_U, A.BC_NS_RHO, A.BC_ANS_U, A.BC_ANS_RHO, A.BC_AAD_RHO, A.BC_NSIN_U, A.BC_NSIN_RHO, A.BC_ANSIN_U,
+           A.BC_EL_STRESS, A.BC_AEL_STRESS)
 
 
 def replay(o, L, f, g, ops, n, ux=None, uy=None, uz=None, rho=None, tem=None, kappa=None):
@@ -31,6 +32,8 @@ def replay(o, L, f, g, ops, n, ux=None, uy=None, uz=None, rho=None, tem=None, ka
         for nm, cn in (("v0", "c0"), ("v1", "c1"), ("v2", "c2")):
             v = op.get(nm)
             vals[nm] = np.full(n, float(op.get(cn, 0.0))) if v is None else np.ascontiguousarray(v, np.float64)
+        # AEL's traction is divided by the routine's rho argument, carried in v2
+        brho = vals["v2"] if k == A.BC_AEL_STRESS else rho
         o.apply_bc(L, tgt, k, op["axis"], op["pos"], op["dir"], ty, g=(g if k == A.BC_AAD_RHO else None),
-                   ux=ux, uy=uy, uz=uz, rho=rho, tem=tem, diffusivity=kappa, kappa=op.get("kappa", 0.0),
+                   ux=ux, uy=uy, uz=uz, rho=brho, tem=tem, diffusivity=kappa, kappa=op.get("kappa", 0.0),
                    eps=op.get("eps", 0.0), **vals)

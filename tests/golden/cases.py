@@ -29,6 +29,13 @@ library. Reference routines per case:
            four sensitivities
   nsinch   an incompressible Brinkman channel on D2Q9: NSin forward steps (walls, NSin velocity
            inlet and pressure outlet), ANSin adjoint steps, the Brinkman sensitivity
+  el       the elastic routines on D2Q9: EL::MacroCollide / MacroExtendedCollide, AEL::MacroCollide
+           (elastic.h:109-166, adjointelastic.h:96-125), the stress boundary routines on every edge
+           and two interior lines (elastic.h:60-104, adjointelastic.h:48-92), the two initial
+           conditions and AEL::SensitivityCompliance (adjointelastic.h:149-155)
+  elsens   the compliance-sensitivity driver loop of test/elsens.cpp on a small plate: EL forward
+           steps (wall on x = 0, traction on x = lx-1, SmoothCorner) accumulating the displacement,
+           AEL adjoint steps, the compliance sensitivity, Normalize
 """
 import zlib
 
@@ -445,6 +452,139 @@ def nsin_run(lib, inp):
     return out
 
 
+# ---------------------------------------------------------------------------- elastic (D2Q9)
+EL_SHAPE = (9, 9, 7, 1)
+EL_TAU = 0.8
+EL_FWD_NAMES = ("ux", "uy", "sxx", "sxy", "syx", "syy")
+EL_ADJ_NAMES = ("irho", "imx", "imy", "isxx", "isxy", "isyx", "isyy")
+EL_KINDS = ("EL_COLLIDE", "EL_EXTENDED", "AEL_COLLIDE")
+EL_BC_KINDS = ("EL_STRESS", "AEL_STRESS")
+# oracle field names of the elastic macros (AEL irho travels in ip)
+EL_FIELD = dict(ux="ux", uy="uy", sxx="sxx", sxy="sxy", syx="syx", syy="syy", irho="ip", imx="imx", imy="imy",
+                isxx="isxx", isxy="isxy", isyx="isyx", isyy="isyy")
+
+
+def el_inputs(name, what, kind=""):
+    """what: collide / bc / init6 / init7 / sens"""
+    q, nx, ny, nz = EL_SHAPE
+    n = nx * ny
+    rng = _rng(name)
+    d = dict(shape=np.array([q, nx, ny, nz]), what=np.array(what), kind=np.array(kind), f=pops(rng, q, n),
+             rho=field(rng, n, 0.9, 1.1), gamma=field(rng, n, 0.1, 1.0),
+             type=(rng.integers(0, 3, n) > 0).astype(np.int32), v0=field(rng, n, -0.5, 0.5),
+             v1=field(rng, n, -0.5, 0.5), dfds=field(rng, n, -1, 1))
+    for nm in EL_FWD_NAMES + EL_ADJ_NAMES:
+        d["in_" + nm] = field(rng, n, -0.5, 0.5)
+    return d
+
+
+def el_fields(lib, inp, prefix):
+    kw = {EL_FIELD[nm]: inp[prefix + nm] for nm in EL_FWD_NAMES + EL_ADJ_NAMES}
+    return lib.fields(rho=inp["rho"], gamma=inp["gamma"], **kw)
+
+
+def el_bc_ops(inp):
+    q, nx, ny, nz = _shape(inp)
+    kind = str(inp["kind"])
+    return [dict(kind=getattr(A, "BC_" + kind), lat=0, axis=a, pos=p, dir=d, type=inp["type"], v0=inp["v0"],
+                 v1=inp["v1"], v2=inp["rho"]) for (a, p, d) in faces_with_interior(q, nx, ny, nz)]
+
+
+def el_run(lib, inp):
+    q, nx, ny, nz = _shape(inp)
+    L = lib.lat(q, nx, ny, 1)
+    n = nx * ny
+    what = str(inp["what"])
+    f = inp["f"].copy()
+    if what == "collide":
+        kind = getattr(A, str(inp["kind"]))
+        out = {nm: np.zeros(n) for nm in EL_FWD_NAMES + EL_ADJ_NAMES}
+        F = lib.fields(rho=inp["rho"], gamma=inp["gamma"], **{EL_FIELD[k]: v for k, v in out.items()})
+        lib.collide(L, kind, f, None, F, tau=EL_TAU, save=True)
+        names = EL_ADJ_NAMES if kind == A.AEL_COLLIDE else EL_FWD_NAMES
+        res = dict(f=f)
+        res.update({"m_" + nm: out[nm] for nm in names})
+        return res
+    if what == "bc":
+        replay(lib, L, f, None, el_bc_ops(inp), n)
+        return dict(f=f)
+    if what in ("init6", "init7"):
+        g = np.zeros((q, n))
+        lib.init(L, int(what[-1]), g, el_fields(lib, inp, "in_"))
+        return dict(f=g)
+    dfds = inp["dfds"].copy()
+    lib.sensitivity(L, 4, dfds, el_fields(lib, inp, "in_"), None)
+    return dict(dfds=dfds)
+
+
+ELS_SHAPE = (9, 21, 15, 1)
+ELS_FWD_STEPS, ELS_ADJ_STEPS = 40, 30
+ELS_STRESS0 = -0.01
+
+
+def elsens_program(kind, nx, ny, rho):
+    """test/elsens.cpp:61-66 (forward) and 75-84 (adjoint): BARRIER where i == 0 on the whole
+    boundary, the traction ty = STRESS0 on the middle of x = nx-1 (zero elsewhere) on every node
+    with i != 0, then SmoothCorner."""
+    n = nx * ny
+    ii = np.tile(np.arange(nx), ny)
+    jj = np.repeat(np.arange(ny), nx)
+    wall = (ii == 0).astype(np.int32)
+    sel = (ii != 0).astype(np.int32)
+    ty = np.where((ii == nx - 1) & (np.abs(jj - 0.5 * ny) < 0.2 * ny), ELS_STRESS0, 0.0)
+    edges = [(0, 0, -1), (0, nx - 1, 1), (1, 0, -1), (1, ny - 1, 1)]
+    wk, sk = (A.BC_WALL, A.BC_EL_STRESS) if kind == "forward" else (A.BC_IWALL, A.BC_AEL_STRESS)
+    ops = [dict(kind=wk, lat=0, axis=a, pos=p, dir=d, type=wall) for (a, p, d) in edges]
+    ops += [dict(kind=sk, lat=0, axis=a, pos=p, dir=d, type=sel, v0=np.zeros(n), v1=ty, v2=rho) for (a, p, d) in edges]
+    ops.append(dict(kind=A.SMOOTH_CORNER, lat=0))
+    return ops
+
+
+def elsens_inputs(name):
+    q, nx, ny, nz = ELS_SHAPE
+    n = nx * ny
+    rng = _rng(name)
+    ii = np.tile(np.arange(nx), ny).astype(np.float64)
+    jj = np.repeat(np.arange(ny), nx).astype(np.float64)
+    s = np.where((ii - 0.5 * nx) ** 2 + jj ** 2 < (0.3 * nx) ** 2, 0.1, 0.9)
+    return dict(rho=1.0 + 0.05 * rng.uniform(-1, 1, n), gamma=s ** 0.25)
+
+
+def elsens_run(lib, inp):
+    """EL::MacroExtendedCollide, Stream and the forward calls for ELS_FWD_STEPS (accumulating
+    rx += ux, ry += uy after each step), AEL::MacroCollide, iStream and the adjoint calls for
+    ELS_ADJ_STEPS, AEL::SensitivityCompliance and Normalize (test/elsens.cpp:52-92)."""
+    q, nx, ny, nz = ELS_SHAPE
+    n = nx * ny
+    L = lib.lat(q, nx, ny, 1)
+    z = np.zeros(n)
+    f = np.zeros((q, n))
+    mac = {nm: np.zeros(n) for nm in EL_FWD_NAMES + EL_ADJ_NAMES}
+    F = lib.fields(rho=inp["rho"], gamma=inp["gamma"], **{EL_FIELD[k]: v for k, v in mac.items()})
+    lib.init(L, 6, f, lib.fields(rho=inp["rho"], ux=z, uy=z, sxx=z, sxy=z, syx=z, syy=z))
+    rx, ry = np.zeros(n), np.zeros(n)
+    ops = elsens_program("forward", nx, ny, inp["rho"])
+    for _ in range(ELS_FWD_STEPS):
+        lib.collide(L, A.EL_EXTENDED, f, None, F, tau=EL_TAU, save=True)
+        lib.stream(L, f)
+        replay(lib, L, f, None, ops, n)
+        rx += mac["ux"]
+        ry += mac["uy"]
+    fa = np.zeros((q, n))
+    lib.init(L, 7, fa, lib.fields(ip=z, imx=z, imy=z, isxx=z, isxy=z, isyx=z, isyy=z, gamma=inp["gamma"]))
+    ops = elsens_program("adjoint", nx, ny, inp["rho"])
+    for _ in range(ELS_ADJ_STEPS):
+        lib.collide(L, A.AEL_COLLIDE, fa, None, F, tau=EL_TAU, save=True)
+        lib.stream(L, fa, True)
+        replay(lib, L, fa, None, ops, n)
+    dfds = np.zeros(n)
+    lib.sensitivity(L, 4, dfds, F, None)
+    lib.normalize(dfds)
+    out = dict(f=f, fa=fa, rx=rx, ry=ry, dfds=dfds)
+    out.update({"m_" + k: v for k, v in mac.items()})
+    return out
+
+
 # ---------------------------------------------------------------------------- registry
 def all_cases():
     """name -> (make_inputs, run)."""
@@ -480,6 +620,16 @@ def all_cases():
         nm = "hsadj_%s" % sk
         cases[nm] = (lambda nm=nm, sk=sk: hs_inputs(nm, sk), hsadj_run)
     cases["nsinch_q9"] = (lambda: nsin_inputs("nsinch_q9"), nsin_run)
+    for kind in EL_KINDS:
+        nm = "el_collide_" + kind
+        cases[nm] = (lambda nm=nm, kind=kind: el_inputs(nm, "collide", kind), el_run)
+    for kind in EL_BC_KINDS:
+        nm = "el_bc_" + kind
+        cases[nm] = (lambda nm=nm, kind=kind: el_inputs(nm, "bc", kind), el_run)
+    for what in ("init6", "init7", "sens"):
+        nm = "el_" + what
+        cases[nm] = (lambda nm=nm, what=what: el_inputs(nm, what), el_run)
+    cases["elsens_q9"] = (lambda: elsens_inputs("elsens_q9"), elsens_run)
     for nc in (1, 2, 3):
         nm = "resid_%d" % nc
         cases[nm] = (lambda nm=nm, nc=nc: resid_inputs(nm, nc), resid_run)

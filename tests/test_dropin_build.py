@@ -29,7 +29,7 @@ def _compile(src, out, extra=()):
     assert p.returncode == 0, p.stderr[-4000:]
 
 
-@pytest.mark.parametrize("driver", ["heatsink_driver", "nsin_channel_driver"])
+@pytest.mark.parametrize("driver", ["heatsink_driver", "nsin_channel_driver", "elastic_driver"])
 def test_test_driver_builds(tmp_path, driver):
     _compile(os.path.join(ROOT, "tests", "dropin", driver + ".cpp"), str(tmp_path / driver))
 
@@ -44,6 +44,25 @@ def test_reference_production_driver_builds_unchanged(tmp_path, driver):
     # the reference's own code trips -Wall here and there: build it as the reference does, quietly
     cmd = [CXX, "-std=c++17", "-O1", "-w", "-I", os.path.join(ROOT, "include"), "-DPANSLBM2_REF=" + ref]
     src, out = str(tmp_path / "production" / (driver + ".cpp")), str(tmp_path / driver)
+    if os.path.exists(LIB):
+        cmd += [src, "-L", LIBDIR, "-lpanslbm_gb300", "-o", out]
+    else:
+        cmd += ["-c", src, "-o", out]
+    p = subprocess.run(cmd, capture_output=True, text=True)
+    assert p.returncode == 0, p.stderr[-4000:]
+
+
+@pytest.mark.skipif(obuild.reference_root() is None, reason="reference sources not present")
+@pytest.mark.parametrize("driver", ["elsens"])
+def test_reference_test_driver_builds_unchanged(tmp_path, driver):
+    """The reference's own elastic sensitivity driver (test/elsens.cpp: EL, AEL, Normalize and the
+    XML exporter) compiles against the drop-in headers unchanged."""
+    ref = obuild.reference_root()
+    (tmp_path / "test").mkdir()
+    shutil.copy(os.path.join(ref, "test", driver + ".cpp"), tmp_path / "test")
+    os.symlink(os.path.join(ROOT, "dropin", "src"), tmp_path / "src")
+    cmd = [CXX, "-std=c++17", "-O1", "-w", "-I", os.path.join(ROOT, "include"), "-DPANSLBM2_REF=" + ref]
+    src, out = str(tmp_path / "test" / (driver + ".cpp")), str(tmp_path / driver)
     if os.path.exists(LIB):
         cmd += [src, "-L", LIBDIR, "-lpanslbm_gb300", "-o", out]
     else:

@@ -126,3 +126,44 @@ def test_dropin_incompressible_channel(nsin_driver, tmp_path):
         close(got[o:o + n], out["m_" + nm], 1e-11)
         o += n
     close(got[o:o + n], out["sens"], 1e-10)
+
+
+@pytest.fixture(scope="module")
+def elastic_driver(tmp_path_factory):
+    cxx = shutil.which("g++")
+    if cxx is None:
+        pytest.skip("g++ not found")
+    out = str(tmp_path_factory.mktemp("dropin") / "elastic_driver")
+    cmd = [cxx, "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"),
+           os.path.join(ROOT, "tests", "dropin", "elastic_driver.cpp"), "-L", LIBDIR, "-lpanslbm_gb300",
+           "-Wl,-rpath," + LIBDIR, "-o", out]
+    subprocess.check_call(cmd)
+    return out
+
+
+def test_dropin_elastic_compliance(elastic_driver, tmp_path):
+    """The loops of the reference's test/elsens.cpp (EL forward with the displacement summed on
+    the host, AEL adjoint, the compliance sensitivity, Normalize) written against the template API
+    reproduce the reference's own loop (tests/golden/elsens_q9.npz)."""
+    inp, out = C.load(os.path.join(ROOT, "tests", "golden", "elsens_q9.npz"))
+    q, nx, ny, _ = C.ELS_SHAPE
+    n = nx * ny
+    fin, fout = tmp_path / "in.bin", tmp_path / "out.bin"
+    with open(fin, "wb") as fh:
+        fh.write(struct.pack("4i", nx, ny, C.ELS_FWD_STEPS, C.ELS_ADJ_STEPS))
+        fh.write(struct.pack("2d", C.EL_TAU, C.ELS_STRESS0))
+        for nm in ("rho", "gamma"):
+            fh.write(np.ascontiguousarray(inp[nm], np.float64).tobytes())
+    subprocess.check_call([elastic_driver, str(fin), str(fout)])
+    got = np.fromfile(fout, np.float64)
+    close(got[:q * n], out["f"], 1e-11)
+    o = q * n
+    for nm in ("rx", "ry", "m_ux", "m_uy", "m_sxx", "m_sxy", "m_syx", "m_syy"):
+        close(got[o:o + n], out[nm], 1e-11)
+        o += n
+    close(got[o:o + q * n], out["fa"], 1e-11)
+    o += q * n
+    for nm in ("irho", "imx", "imy", "isxx", "isxy", "isyx", "isyy"):
+        close(got[o:o + n], out["m_" + nm], 1e-11)
+        o += n
+    close(got[o:o + n], out["dfds"], 1e-10)

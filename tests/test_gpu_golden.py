@@ -264,3 +264,108 @@ def test_incompressible_kinds_are_d2q9_only():
     with pytest.raises(A.PanslbmError, match="D2Q9 only"):
         lp.program(HS.to_descs([dict(kind=A.BC_NSIN_U, axis=0, pos=0, dir=-1)]))
     lp.close()
+
+
+def _el_lattice(inp, storage="fp64"):
+    q, nx, ny, _ = C._shape(inp)
+    return LatticePair(q, nx, ny, 1, storage), nx * ny
+
+
+@_files("el")
+@pytest.mark.parametrize("storage", ["fp64", "fp32"])
+def test_elastic_routines(path, storage):
+    """EL / AEL collides, stress boundary routines, initial conditions and the compliance
+    sensitivity against the reference's outputs: FP64 to 1e-12 (bit-exact arithmetic order, the
+    stress routines divide), FP32 compute to 2e-6 of the field's largest magnitude."""
+    inp, out = C.load(path)
+    lp, n = _el_lattice(inp, storage)
+    tol = RTOL if storage == "fp64" else 2e-6
+    what = str(inp["what"])
+    lp.set_field(A.DENSITY, inp["rho"])
+    lp.set_field(A.GAMMA, inp["gamma"])
+    if what == "collide":
+        kind = getattr(A, str(inp["kind"]))
+        lp.set_populations(0, inp["f"])
+        lp.collide(kind, phys(tau=C.EL_TAU), save=True)
+        close(lp.get_populations(0), out["f"], tol)
+        fids = dict(ux=A.UX, uy=A.UY, sxx=A.SXX, sxy=A.SXY, syx=A.SYX, syy=A.SYY, irho=A.IRHO, imx=A.IMX, imy=A.IMY,
+                    isxx=A.ISXX, isxy=A.ISXY, isyx=A.ISYX, isyy=A.ISYY)
+        for nm in (C.EL_ADJ_NAMES if kind == A.AEL_COLLIDE else C.EL_FWD_NAMES):
+            close(lp.get_field(fids[nm]), out["m_" + nm], tol * 10)
+    elif what == "bc":
+        lp.set_populations(0, inp["f"])
+        prog = lp.program(HS.to_descs(C.el_bc_ops(inp)))
+        lp.stream(mode=3 if str(inp["kind"]) == "AEL_STRESS" else 2, prog=prog, both=False)
+        close(lp.get_populations(0), out["f"], tol)
+    elif what in ("init6", "init7"):
+        names = C.EL_FWD_NAMES if what == "init6" else C.EL_ADJ_NAMES
+        arrays = [inp["rho"]] + [inp["in_" + nm] for nm in names] if what == "init6" else \
+            [inp["in_" + nm] for nm in names]
+        lp.init_elastic(0 if what == "init6" else 1, arrays)
+        close(lp.get_populations(0), out["f"], tol)
+    else:
+        arrays = [inp["in_" + nm] for nm in ("sxx", "sxy", "syx", "syy", "irho", "isxx", "isxy", "isyx", "isyy")]
+        got = lp.sensitivity_compliance(inp["dfds"], arrays)
+        if storage == "fp64":
+            assert np.array_equal(got, out["dfds"])   # rounded term by term, like the reference
+        else:
+            close(got, out["dfds"], tol)
+    lp.close()
+
+
+@_files("elsens")
+@pytest.mark.parametrize("fused", [True, False])
+def test_elastic_compliance_driver(path, fused):
+    """test/elsens.cpp on a small plate: EL forward steps (fused pull + boundary program +
+    MacroExtendedCollide, or collide and stream calls separately) with the displacement summed
+    over the steps, AEL adjoint steps, the compliance sensitivity from the saved macros on the
+    device and Normalize, against the reference's own loop."""
+    inp, out = C.load(path)
+    q, nx, ny, _ = C.ELS_SHAPE
+    n = nx * ny
+    lp = LatticePair(q, nx, ny, 1, "fp64")
+    ph = phys(tau=C.EL_TAU)
+    z = np.zeros(n)
+    lp.set_field(A.DENSITY, inp["rho"])
+    lp.set_field(A.GAMMA, inp["gamma"])
+    lp.init_elastic(0, [inp["rho"], z, z, z, z, z, z])
+    prog = lp.program(HS.to_descs(C.elsens_program("forward", nx, ny, inp["rho"])))
+    rx, ry = np.zeros(n), np.zeros(n)
+    for t in range(C.ELS_FWD_STEPS):
+        if t == 0 or not fused:
+            lp.collide(A.EL_EXTENDED, ph, save=True)
+        else:
+            lp.step(A.EL_EXTENDED, ph, prog, save=True)
+        rx += lp.get_field(A.UX)
+        ry += lp.get_field(A.UY)
+        if not fused or t == C.ELS_FWD_STEPS - 1:
+            lp.stream(mode=0, prog=prog, both=False)
+    close(lp.get_populations(0), out["f"], 1e-11)
+    close(rx, out["rx"], 1e-11)
+    close(ry, out["ry"], 1e-11)
+    for fid, nm in ((A.UX, "ux"), (A.UY, "uy"), (A.SXX, "sxx"), (A.SXY, "sxy"), (A.SYX, "syx"), (A.SYY, "syy")):
+        close(lp.get_field(fid), out["m_" + nm], 1e-11)
+    lp.init_elastic(1, [z] * 7)
+    prog = lp.program(HS.to_descs(C.elsens_program("adjoint", nx, ny, inp["rho"])))
+    for t in range(C.ELS_ADJ_STEPS):
+        if t == 0 or not fused:
+            lp.collide(A.AEL_COLLIDE, ph, save=True)
+        else:
+            lp.step(A.AEL_COLLIDE, ph, prog, save=True)
+        if not fused or t == C.ELS_ADJ_STEPS - 1:
+            lp.stream(mode=1, prog=prog, both=False)
+    close(lp.get_populations(0), out["fa"], 1e-11)
+    for fid, nm in ((A.IRHO, "irho"), (A.IMX, "imx"), (A.IMY, "imy"), (A.ISXX, "isxx"), (A.ISXY, "isxy"),
+                    (A.ISYX, "isyx"), (A.ISYY, "isyy")):
+        close(lp.get_field(fid), out["m_" + nm], 1e-11)
+    close(lp.normalize(lp.sensitivity_compliance(np.zeros(n))), out["dfds"], 1e-10)
+    lp.close()
+
+
+def test_elastic_kinds_are_d2q9_only():
+    lp = LatticePair(15, 6, 5, 4, "fp64")
+    with pytest.raises(A.PanslbmError, match="D2Q9 only"):
+        lp.collide(A.EL_COLLIDE, phys(tau=0.8))
+    with pytest.raises(A.PanslbmError, match="D2Q9 only"):
+        lp.program(HS.to_descs([dict(kind=A.BC_EL_STRESS, axis=0, pos=0, dir=-1)]))
+    lp.close()
