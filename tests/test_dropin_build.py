@@ -1,6 +1,7 @@
 """The drop-in headers (dropin/src) compile as PANSLBM2's template API: the heat-sink test
 driver written against that API, and, where the reference sources are present, the reference's
 own production drivers unchanged (copied to a scratch directory whose ../src is dropin/src).
+The drop-in tree is self-contained: no header of the reference is on the include path.
 No GPU needed: compile and link only."""
 import os
 import shutil
@@ -42,7 +43,7 @@ def test_reference_production_driver_builds_unchanged(tmp_path, driver):
     shutil.copy(os.path.join(ref, "production", driver + ".cpp"), tmp_path / "production")
     os.symlink(os.path.join(ROOT, "dropin", "src"), tmp_path / "src")
     # the reference's own code trips -Wall here and there: build it as the reference does, quietly
-    cmd = [CXX, "-std=c++17", "-O1", "-w", "-I", os.path.join(ROOT, "include"), "-DPANSLBM2_REF=" + ref]
+    cmd = [CXX, "-std=c++17", "-O1", "-w", "-I", os.path.join(ROOT, "include")]
     src, out = str(tmp_path / "production" / (driver + ".cpp")), str(tmp_path / driver)
     if os.path.exists(LIB):
         cmd += [src, "-L", LIBDIR, "-lpanslbm_gb300", "-o", out]
@@ -61,7 +62,7 @@ def test_reference_test_driver_builds_unchanged(tmp_path, driver):
     (tmp_path / "test").mkdir()
     shutil.copy(os.path.join(ref, "test", driver + ".cpp"), tmp_path / "test")
     os.symlink(os.path.join(ROOT, "dropin", "src"), tmp_path / "src")
-    cmd = [CXX, "-std=c++17", "-O1", "-w", "-I", os.path.join(ROOT, "include"), "-DPANSLBM2_REF=" + ref]
+    cmd = [CXX, "-std=c++17", "-O1", "-w", "-I", os.path.join(ROOT, "include")]
     src, out = str(tmp_path / "test" / (driver + ".cpp")), str(tmp_path / driver)
     if os.path.exists(LIB):
         cmd += [src, "-L", LIBDIR, "-lpanslbm_gb300", "-o", out]
