@@ -128,6 +128,11 @@ extern "C" {
 #define PL_FWD_UY 34
 #define PL_FWD_UZ 35
 #define PL_FWD_TEM 36
+#define PL_DFDS 37      /* device sensitivity accumulator of pl_sensitivity_device          */
+#define PL_DADS 38      /* its inputs dalpha/ds, dkappa/ds and the heat-source flux qn       */
+#define PL_DKDS 39
+#define PL_QN 40
+#define PL_ACC 41       /* a free accumulator for pl_accumulate                              */
 
 typedef struct pl_lattice_s *pl_lattice;
 
@@ -249,6 +254,29 @@ int pl_residual_device_noalloc(long long n, int ncomp, const double *const *a, c
  * reads PL_FWD_* (forward), the adjoint macros, PL_KAPPA and the two snapshots. */
 int pl_sensitivity(pl_lattice h, int which, double *dfds, const double *dads, const double *dkds, const double *qn,
                    const int *mask);
+
+/* Checkpointed sweeps (no counterpart in the reference, whose transient drivers keep every time
+ * step's fields in host memory, production/heatsink_transient.cpp:45-52): device-resident stores,
+ * numbered slots allocated on first use and kept until pl_store_release / pl_destroy.
+ *   PL_STORE_POPS  both population sets of the current buffer (a checkpoint);
+ *   PL_STORE_FWD   rho, ux, uy, uz, T saved by the last saving forward collide; pl_load puts them
+ *                  in PL_FWD_* (the adjoint collides' and adjoint routines' forward inputs);
+ *   PL_STORE_SNAP  the forward g snapshot (pl_snapshot slot 0); pl_load puts it back in slot 0. */
+#define PL_STORE_POPS 0
+#define PL_STORE_FWD 1
+#define PL_STORE_SNAP 2
+int pl_store(pl_lattice h, int what, int slot);
+int pl_load(pl_lattice h, int what, int slot);
+int pl_store_release(pl_lattice h);
+/* pl_sensitivity on the device: accumulates into the device field PL_DFDS (reset it with
+ * pl_set_field, read it with pl_get_field), so a transient sweep adds one term per time step
+ * (production/heatsink_transient.cpp:191-194) without host traffic. dads, dkds, qn and mask are
+ * uploaded when non-NULL and reused by later calls when NULL. */
+int pl_sensitivity_device(pl_lattice h, int which, const double *dads, const double *dkds, const double *qn,
+                          const int *mask);
+/* dst += a * src over the lattice: dst a device accumulator (PL_DFDS..PL_ACC), src any field
+ * pl_get_field reads (e.g. PL_TEM of the last saving collide, for a time-integrated objective) */
+int pl_accumulate(pl_lattice h, int dst, int src, double a);
 
 /* AEL::SensitivityCompliance (adjointelastic.h:149-155), D2Q9: dfds (host, N) is accumulated
  * into; in = nine host arrays sxx, sxy, syx, syy, irho, isxx, isxy, isyx, isyy, or NULL for the

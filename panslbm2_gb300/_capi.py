@@ -32,6 +32,8 @@ OPT_GRAPHS, OPT_SIDE_PRIORITY = 1, 2
 RHO, UX, UY, UZ, TEM, QX, QY, QZ = 8, 9, 10, 11, 12, 13, 14, 15
 IP, IUX, IUY, IUZ, IMX, IMY, IMZ, ITEM, IQX, IQY, IQZ = 16, 17, 18, 19, 20, 21, 22, 23, 24, 25, 26
 FWD_RHO, FWD_UX, FWD_UY, FWD_UZ, FWD_TEM = 32, 33, 34, 35, 36
+DFDS, DADS, DKDS, QN, ACC = 37, 38, 39, 40, 41
+STORE_POPS, STORE_FWD, STORE_SNAP = 0, 1, 2
 # the elastic kinds' macros share the planes above
 SXX, SXY, SYX, SYY = TEM, QX, QY, QZ
 IRHO, ISXX, ISXY, ISYX, ISYY = IP, ITEM, IQX, IQY, IQZ
@@ -58,7 +60,8 @@ EXPORTS = [
     "pl_set_populations", "pl_get_populations", "pl_set_field", "pl_get_field", "pl_freeze_forward",
     "pl_program_create", "pl_program_destroy", "pl_init", "pl_init_elastic", "pl_collide", "pl_step", "pl_steps", "pl_stream",
     "pl_solve", "pl_snapshot", "pl_set_snapshot", "pl_residual", "pl_residual_host", "pl_residual_device_noalloc",
-    "pl_sensitivity", "pl_sensitivity_compliance", "pl_heaviside_var",
+    "pl_sensitivity", "pl_sensitivity_compliance", "pl_store", "pl_load", "pl_store_release",
+    "pl_sensitivity_device", "pl_accumulate", "pl_heaviside_var",
     "pl_heaviside_sens", "pl_density_filter", "pl_normalize", "pl_stats", "pl_mma_create", "pl_mma_set_param",
     "pl_mma_update", "pl_mma_destroy", "pl_mma_get_state", "pl_mma_set_state",
 ]

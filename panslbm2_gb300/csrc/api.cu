@@ -120,6 +120,9 @@ struct pl_lattice_s {
     int side_prio = 0, prio_lo = 0, prio_hi = 0;
     std::map<GraphKey, GraphEntry> graphs;
     bool use_graphs = true;
+    // device stores of a checkpointed sweep, per kind (populations, forward macros, snapshot)
+    std::vector<void *> store[3];
+    int *sens_mask = nullptr;        // source mask of pl_sensitivity_device
 };
 
 namespace {
@@ -836,6 +839,8 @@ int pl_destroy(pl_lattice h) {
     for (int s = 0; s < 2; ++s) { for (auto *p : h->fwd[s]) cudaFree(p); for (auto *p : h->adj[s]) cudaFree(p); cudaFree(h->snap[s]); }
     for (auto *p : h->scratch) cudaFree(p);
     cudaFree(h->iscratch); cudaFree(h->partial); cudaFree(h->nonfinite); cudaFree(h->err); cudaFree(h->dout);
+    for (auto &v : h->store) for (void *p : v) cudaFree(p);
+    cudaFree(h->sens_mask);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
     if (h->side) { cudaStreamSynchronize(h->side); cudaStreamDestroy(h->side); }
@@ -928,7 +933,7 @@ int pl_get_populations(pl_lattice h, int set, double *host) {
 int pl_set_field(pl_lattice h, int f, const double *host) {
     if (!h || !host) return fail(PL_ERR_ARG, "bad arguments");
     int r;
-    if ((f >= PL_ALPHA && f <= PL_GAMMA) || (f >= PL_FWD_RHO && f <= PL_FWD_TEM)) {
+    if ((f >= PL_ALPHA && f <= PL_GAMMA) || (f >= PL_FWD_RHO && f <= PL_ACC)) {
         if ((r = ensure_d(h, &h->fld[f], h->n))) return r;
         if ((r = upload(h, h->fld[f], host, h->n))) return r;
         return sync_cfield(h, f);
@@ -951,7 +956,7 @@ int pl_set_field(pl_lattice h, int f, const double *host) {
 int pl_get_field(pl_lattice h, int f, double *host) {
     if (!h || !host) return fail(PL_ERR_ARG, "bad arguments");
     const double *src = nullptr;
-    if ((f >= PL_ALPHA && f <= PL_GAMMA) || (f >= PL_FWD_RHO && f <= PL_FWD_TEM)) src = h->fld[f];
+    if ((f >= PL_ALPHA && f <= PL_GAMMA) || (f >= PL_FWD_RHO && f <= PL_ACC)) src = h->fld[f];
     else if (f >= PL_RHO && f <= PL_QZ) src = h->fwd_saved >= 0 ? h->fwd[h->fwd_saved][f - PL_RHO] : nullptr;
     else if (f >= PL_IP && f <= PL_IQZ) src = h->adj_saved >= 0 ? h->adj[h->adj_saved][f - PL_IP] : nullptr;
     else return fail(PL_ERR_ARG, "unknown field %d", f);
@@ -1335,6 +1340,121 @@ int pl_sensitivity_compliance(pl_lattice h, double *dfds, const double *const *i
     pl::launch_compliance(h->n, buf, dev, h->st);
     if ((r = check_launch(h, 1))) return r;
     return download(h, dfds, buf, h->n);
+}
+
+// ---- checkpointed sweeps --------------------------------------------------------------------
+static size_t store_bytes(pl_lattice h, int what) {
+    if (what == PL_STORE_POPS) return (size_t)2 * h->q * h->np * h->ssize;
+    if (what == PL_STORE_FWD) return sizeof(double) * 5 * (size_t)h->n;
+    return sizeof(double) * (size_t)h->q * h->np;
+}
+
+int pl_store(pl_lattice h, int what, int slot) {
+    if (!h || what < PL_STORE_POPS || what > PL_STORE_SNAP || slot < 0) return fail(PL_ERR_ARG, "bad arguments");
+    std::vector<void *> &v = h->store[what];
+    if ((int)v.size() <= slot) v.resize(slot + 1, nullptr);
+    int r;
+    const size_t bytes = store_bytes(h, what);
+    if (!v[slot] && (r = dalloc(&v[slot], bytes))) return r;
+    char *dst = static_cast<char *>(v[slot]);
+    if (what == PL_STORE_POPS) {
+        CK(cudaMemcpyAsync(dst, h->pop[h->cur], bytes, cudaMemcpyDeviceToDevice, h->st));
+    } else if (what == PL_STORE_FWD) {
+        if (h->fwd_saved < 0) return fail(PL_ERR_STATE, "no saved forward collide");
+        for (int m = 0; m < 5; ++m) {
+            const double *src = h->fwd[h->fwd_saved][m];
+            double *d = reinterpret_cast<double *>(dst) + (size_t)m * h->n;
+            if (src) { CK(cudaMemcpyAsync(d, src, sizeof(double) * h->n, cudaMemcpyDeviceToDevice, h->st)); }
+            else { CK(cudaMemsetAsync(d, 0, sizeof(double) * h->n, h->st)); }
+        }
+    } else {
+        if (!h->snap[0]) return fail(PL_ERR_STATE, "no forward snapshot (pl_snapshot slot 0)");
+        CK(cudaMemcpyAsync(dst, h->snap[0], bytes, cudaMemcpyDeviceToDevice, h->st));
+    }
+    return PL_OK;
+}
+
+int pl_load(pl_lattice h, int what, int slot) {
+    if (!h || what < PL_STORE_POPS || what > PL_STORE_SNAP || slot < 0) return fail(PL_ERR_ARG, "bad arguments");
+    const std::vector<void *> &v = h->store[what];
+    if ((int)v.size() <= slot || !v[slot]) return fail(PL_ERR_STATE, "store %d slot %d is empty", what, slot);
+    const char *src = static_cast<const char *>(v[slot]);
+    int r;
+    if (what == PL_STORE_POPS) {
+        CK(cudaMemcpyAsync(h->pop[h->cur], src, store_bytes(h, what), cudaMemcpyDeviceToDevice, h->st));
+        h->last_kind = -1;
+    } else if (what == PL_STORE_FWD) {
+        for (int m = 0; m < 5; ++m) {
+            const int f = PL_FWD_RHO + m;
+            if ((r = ensure_d(h, &h->fld[f], h->n))) return r;
+            CK(cudaMemcpyAsync(h->fld[f], reinterpret_cast<const double *>(src) + (size_t)m * h->n, sizeof(double) * h->n,
+                               cudaMemcpyDeviceToDevice, h->st));
+            if ((r = sync_cfield(h, f))) return r;
+        }
+    } else {
+        if ((r = ensure_d(h, &h->snap[0], (size_t)h->q * h->np))) return r;
+        CK(cudaMemcpyAsync(h->snap[0], src, store_bytes(h, what), cudaMemcpyDeviceToDevice, h->st));
+    }
+    return PL_OK;
+}
+
+int pl_store_release(pl_lattice h) {
+    if (!h) return fail(PL_ERR_ARG, "null handle");
+    CK(cudaStreamSynchronize(h->st));
+    for (auto &v : h->store) { for (void *p : v) cudaFree(p); v.clear(); }
+    return PL_OK;
+}
+
+int pl_sensitivity_device(pl_lattice h, int which, const double *dads, const double *dkds, const double *qn,
+                          const int *mask) {
+    if (!h || which < 0 || which > 3) return fail(PL_ERR_ARG, "bad arguments");
+    if (h->adj_saved < 0) return fail(PL_ERR_STATE, "no saved adjoint collide");
+    if (which <= 1 && (!h->snap[0] || !h->snap[1])) return fail(PL_ERR_STATE, "take both snapshots (pl_snapshot) first");
+    for (int f = PL_FWD_RHO; f <= PL_FWD_TEM; ++f)
+        if (!h->fld[f]) return fail(PL_ERR_STATE, "forward solution not set (pl_freeze_forward / pl_load)");
+    int r;
+    const double *hin[3] = {dads, dkds, qn};
+    for (int m = 0; m < 3; ++m) {
+        const int f = PL_DADS + m;
+        if (hin[m]) {
+            if ((r = ensure_d(h, &h->fld[f], h->n)) || (r = upload(h, h->fld[f], hin[m], h->n))) return r;
+        }
+    }
+    if (mask) {
+        if (!h->sens_mask && (r = dalloc((void **)&h->sens_mask, sizeof(int) * h->n))) return r;
+        CK(cudaMemcpyAsync(h->sens_mask, mask, sizeof(int) * h->n, cudaMemcpyHostToDevice, h->st));
+    }
+    if (!h->fld[PL_DADS] || (which <= 2 && !h->fld[PL_DKDS]) || (which == 0 && (!h->fld[PL_QN] || !h->sens_mask)))
+        return fail(PL_ERR_STATE, "sensitivity inputs not given yet");
+    if ((r = ensure_d(h, &h->fld[PL_DFDS], h->n))) return r;
+    if ((r = ensure_d(h, &h->fld[PL_KAPPA], h->n))) return r;
+    pl::SensArgs sa;
+    memset(&sa, 0, sizeof sa);
+    sa.which = which; sa.n = h->n; sa.nx = h->nx; sa.ny = h->ny; sa.nz = h->nz; sa.np = h->np;
+    sa.dfds = h->fld[PL_DFDS]; sa.dads = h->fld[PL_DADS]; sa.dkds = h->fld[PL_DKDS]; sa.qn = h->fld[PL_QN];
+    sa.mask = h->sens_mask;
+    sa.ux = h->fld[PL_FWD_UX]; sa.uy = h->fld[PL_FWD_UY]; sa.uz = h->fld[PL_FWD_UZ]; sa.tem = h->fld[PL_FWD_TEM];
+    const int as = h->adj_saved;
+    sa.imx = h->adj[as][4]; sa.imy = h->adj[as][5]; sa.imz = h->adj[as][6];
+    sa.item = h->adj[as][7]; sa.iqx = h->adj[as][8]; sa.iqy = h->adj[as][9]; sa.iqz = h->adj[as][10];
+    sa.kappa = h->fld[PL_KAPPA];
+    sa.g = h->snap[0]; sa.ig = h->snap[1];
+    pl::launch_sensitivity(h->q, sa, h->st);
+    return check_launch(h, 1);
+}
+
+int pl_accumulate(pl_lattice h, int dst, int src, double a) {
+    if (!h || dst < PL_DFDS || dst > PL_ACC) return fail(PL_ERR_ARG, "bad arguments");
+    const double *s = nullptr;
+    if ((src >= PL_ALPHA && src <= PL_GAMMA) || (src >= PL_FWD_RHO && src <= PL_ACC)) s = h->fld[src];
+    else if (src >= PL_RHO && src <= PL_QZ) s = h->fwd_saved >= 0 ? h->fwd[h->fwd_saved][src - PL_RHO] : nullptr;
+    else if (src >= PL_IP && src <= PL_IQZ) s = h->adj_saved >= 0 ? h->adj[h->adj_saved][src - PL_IP] : nullptr;
+    else return fail(PL_ERR_ARG, "unknown field %d", src);
+    if (!s) return fail(PL_ERR_STATE, "field %d has no value yet", src);
+    int r;
+    if ((r = ensure_d(h, &h->fld[dst], h->n))) return r;
+    pl::launch_axpy(h->n, h->fld[dst], s, a, h->st);
+    return check_launch(h, 1);
 }
 
 static int filter_common(pl_lattice h, int op, double R, double beta, const double *s, const double *d,

@@ -199,6 +199,14 @@ void launch_compliance(int n, double *dfds, const double *const *in, cudaStream_
     k_compliance<<<(n + kRB - 1) / kRB, kRB, 0, st>>>(n, dfds, c);
 }
 
+__global__ void k_axpy(int n, double *dst, const double *src, double a) {
+    const int i = blockIdx.x * kRB + threadIdx.x;
+    if (i < n) dst[i] = __dadd_rn(dst[i], __dmul_rn(a, src[i]));
+}
+void launch_axpy(int n, double *dst, const double *src, double a, cudaStream_t st) {
+    k_axpy<<<(n + kRB - 1) / kRB, kRB, 0, st>>>(n, dst, src, a);
+}
+
 // ---- filters ------------------------------------------------------------------------------
 // Taps of the (2 nR + 1)^d box with distance <= R, in the reference's (i2, j2, k2) loop order,
 // with their hat weights (R - dist)/R computed on the host in FP64.

@@ -30,6 +30,8 @@ void launch_sensitivity(int q, const SensArgs &s, cudaStream_t st);
 // AEL::SensitivityCompliance: dfds[i] += 4.5 s:is - 1.5 irho tr s; in = sxx, sxy, syx, syy, irho,
 // isxx, isxy, isyx, isyy (device arrays of n)
 void launch_compliance(int n, double *dfds, const double *const *in, cudaStream_t st);
+// dst[i] += a * src[i]
+void launch_axpy(int n, double *dst, const double *src, double a, cudaStream_t st);
 
 struct FiltArgs {
     int n, nx, ny, nz, ntap;

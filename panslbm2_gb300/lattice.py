@@ -169,6 +169,25 @@ class LatticePair:
         check(self.lib.pl_sensitivity_compliance(self.h, _dp(dfds), P))
         return dfds
 
+    def store(self, what, slot):
+        check(self.lib.pl_store(self.h, what, slot))
+
+    def load(self, what, slot):
+        check(self.lib.pl_load(self.h, what, slot))
+
+    def store_release(self):
+        check(self.lib.pl_store_release(self.h))
+
+    def sensitivity_device(self, which, dads=None, dkds=None, qn=None, mask=None):
+        """accumulate one sensitivity term into the device field DFDS (inputs reused when None)"""
+        dads, dkds, qn = _f64(dads, self.n), _f64(dkds, self.n), _f64(qn, self.n)
+        mask = _i32(mask, self.n)
+        check(self.lib.pl_sensitivity_device(self.h, which, _dp(dads), _dp(dkds), _dp(qn),
+                                             None if mask is None else mask.ctypes.data_as(A.IPT)))
+
+    def accumulate(self, dst, src, a=1.0):
+        check(self.lib.pl_accumulate(self.h, dst, src, C.c_double(a)))
+
     def collide(self, kind, ph, save=True):
         check(self.lib.pl_collide(self.h, kind, C.byref(ph), int(save)))
 

@@ -1,0 +1,124 @@
+"""One transient heat-sink design evaluation on the device, with checkpointed forward states.
+
+The loops of production/heatsink_transient.cpp:135-205 (2D) and heatsink3D_transient.cpp (3D):
+a forward run of nt-1 time steps from rest (NS + AD, natural convection, Brinkman), then the
+adjoint swept backward over the same steps, each adjoint step adding its term of
+AAD::SensitivityTemperatureAtHeatSource, and the time-averaged source temperature as objective.
+
+The reference keeps every time step's rho, u, T and g snapshot in host memory (nt arrays of each,
+heatsink_transient.cpp:45-52). Here the forward run keeps only a checkpoint of the populations
+every `checkpoint_every` steps, on the device (pl_store). The adjoint sweep walks the segments
+backward: it parks the adjoint populations, restores the segment's checkpoint, recomputes the
+segment's forward steps storing their macros and snapshots on the device, brings the adjoint
+populations back and runs the segment's adjoint steps, each reading its step's forward state
+(pl_load). The sensitivity accumulates on the device (pl_sensitivity_device) and the objective's
+time sum too (pl_accumulate); the host sees two arrays at the end.
+
+Step order per adjoint time step t (heatsink_transient.cpp:181-204): AAD collide with the forward
+state of step t, the sensitivity term of step t (forward snapshot gi[t], adjoint snapshot igi),
+then iStream and the adjoint boundary calls with the velocity of step t. The reference's forward
+loop never writes gi[0], which its adjoint reads at t = 0 (allocated but not initialised); here
+that snapshot is zero.
+"""
+import time
+
+import numpy as np
+
+from . import _capi as A
+from . import heatsink as HS
+from .lattice import LatticePair, phys
+
+
+class TransientHeatSink:
+    def __init__(self, p, storage="fp64", checkpoint_every=100):
+        self.p, self.K = p, int(checkpoint_every)
+        self.q = 9 if p.nd == 2 else 15
+        self.n = p.lx * p.ly * p.lz
+        self.lp = LatticePair(self.q, p.lx, p.ly, p.lz, storage)
+        self.prog_f = self.lp.program(HS.to_descs(HS.program_ops("forward", p)))
+        self.prog_a = self.lp.program(HS.to_descs(HS.program_ops("adjoint", p)))
+        self.ph = phys(nu=p.nu, diff=0.0, gx=p.gx, gy=p.gy, gz=p.gz, tem0=p.tem0)
+        self.qn, self.mask = p.source()
+
+    def close(self):
+        self.lp.close()
+
+    def _recompute(self, seg, t_last):
+        """forward steps of segment `seg` (t0 = seg*K + 1 .. t_last) from its checkpoint; their
+        macros and forward snapshots go to device slots t - t0"""
+        lp, ph = self.lp, self.ph
+        lp.load(A.STORE_POPS, seg)
+        t0 = seg * self.K + 1
+        for t in range(t0, t_last + 1):
+            if t == t0:
+                lp.collide(A.AD_NATURAL, ph, save=True)
+            else:
+                lp.step(A.AD_NATURAL, ph, self.prog_f, save=True)
+            lp.snapshot(0, host=False)
+            lp.store(A.STORE_FWD, t - t0)
+            lp.store(A.STORE_SNAP, t - t0)
+
+    def evaluate(self, alpha, kappa, dads, dkds, nt):
+        """objective (time-averaged temperature on the heat source), its sensitivity dfdss and
+        the phase times; nt counts the time levels 0..nt-1 as the reference's loops do"""
+        lp, n, K, nd = self.lp, self.n, self.K, self.p.nd
+        zero, one = np.zeros(n), np.ones(n)
+        times = {}
+        t0 = time.perf_counter()
+        lp.set_field(A.ALPHA, alpha)
+        lp.set_field(A.KAPPA, kappa)
+        lp.set_field(A.ACC, zero)
+        lp.set_field(A.DFDS, zero)
+        # forward (heatsink_transient.cpp:135-170): checkpoints at the segment starts t = 1, K+1, ...
+        lp.init(0, one, ux=zero, uy=zero, uz=zero)
+        lp.init(1, zero, ux=zero, uy=zero, uz=zero)
+        nseg = 0
+        for t in range(1, nt):
+            if (t - 1) % K == 0:
+                if t > 1:
+                    lp.stream(mode=0, prog=self.prog_f, both=True)
+                lp.store(A.STORE_POPS, (t - 1) // K)
+                nseg += 1
+                lp.collide(A.AD_NATURAL, self.ph, save=True)
+            else:
+                lp.step(A.AD_NATURAL, self.ph, self.prog_f, save=True)
+            lp.accumulate(A.ACC, A.TEM)
+        ul = [lp.get_field(A.UX), lp.get_field(A.UY), lp.get_field(A.UZ) if nd == 3 else zero]
+        times["forward"] = time.perf_counter() - t0
+        # adjoint (heatsink_transient.cpp:172-205), segment by segment from the last
+        t1 = time.perf_counter()
+        lp.init(2, zero, zero, zero, zero, ux=ul[0], uy=ul[1], uz=ul[2])
+        lp.init(3, zero, zero, zero, zero, ux=ul[0], uy=ul[1], uz=ul[2])
+        park = nseg   # store slot of the adjoint populations while a segment is recomputed
+        first = True
+        loaded_seg = -1
+        for t in range(nt - 2, -1, -1):
+            if t >= 1:
+                seg = (t - 1) // K
+                if seg != loaded_seg:
+                    lp.store(A.STORE_POPS, park)
+                    self._recompute(seg, min(seg * K + K, nt - 2))
+                    lp.load(A.STORE_POPS, park)
+                    loaded_seg = seg
+                lp.load(A.STORE_FWD, t - (seg * K + 1))
+                lp.load(A.STORE_SNAP, t - (seg * K + 1))
+            else:
+                # time level 0: the state at rest, and no forward snapshot
+                for fid, v in ((A.FWD_RHO, one), (A.FWD_UX, zero), (A.FWD_UY, zero), (A.FWD_UZ, zero),
+                               (A.FWD_TEM, zero)):
+                    lp.set_field(fid, v)
+                lp.set_snapshot(0, np.zeros(n * self.q))
+            lp.collide(A.AAD_NATURAL, self.ph, save=True)
+            lp.snapshot(1, host=False)
+            if first:
+                lp.sensitivity_device(0, dads, dkds, self.qn, self.mask)
+                first = False
+            else:
+                lp.sensitivity_device(0)
+            lp.stream(mode=1, prog=self.prog_a, both=True)
+        dfdss = lp.get_field(A.DFDS)
+        acc = lp.get_field(A.ACC)
+        times["adjoint"] = time.perf_counter() - t1
+        lp.store_release()
+        objective = float(np.sum(acc[self.mask != 0])) / (self.p.L * nt)
+        return dict(objective=objective, dfdss=dfdss, times=times, segments=nseg)

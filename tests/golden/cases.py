@@ -33,6 +33,10 @@ library. Reference routines per case:
            (elastic.h:109-166, adjointelastic.h:96-125), the stress boundary routines on every edge
            and two interior lines (elastic.h:60-104, adjointelastic.h:48-92), the two initial
            conditions and AEL::SensitivityCompliance (adjointelastic.h:149-155)
+  hst      the transient heat-sink loops of production/heatsink_transient.cpp:135-205 on a small
+           lattice: forward from rest keeping every time level's macros and g snapshot, the adjoint
+           swept backward with one SensitivityTemperatureAtHeatSource term per step, and the
+           time-averaged source temperature
   elsens   the compliance-sensitivity driver loop of test/elsens.cpp on a small plate: EL forward
            steps (wall on x = 0, traction on x = lx-1, SmoothCorner) accumulating the displacement,
            AEL adjoint steps, the compliance sensitivity, Normalize
@@ -585,6 +589,74 @@ def elsens_run(lib, inp):
     return out
 
 
+# ---------------------------------------------------------------------------- transient heat sink
+HST_SHAPE = (2, 16, 12, 1)
+HST_LEVELS = 25   # time levels 0..nt-1 (the driver's nt)
+
+
+def hst_params():
+    nd, lx, ly, lz = HST_SHAPE
+    return HS.Params(nd, lx, ly, lz)
+
+
+def hst_inputs(name):
+    p = hst_params()
+    ss = np.clip(HS.grf_design(p.nd, p.lx, p.ly, p.lz, seed=5, sigma=2.0), 0, 1)
+    alpha, kappa, dads, dkds = p.design_fields(ss)
+    return dict(alpha=alpha, kappa=kappa, dads=dads, dkds=dkds)
+
+
+def hst_run(lib, inp):
+    """production/heatsink_transient.cpp:135-205 with every time level kept: rho, u, T and the g
+    snapshot gi[t] of t = 1..nt-1 from the forward loop (t = 0: rest, gi[0] zero), then the adjoint
+    from t = nt-2 down to 0 with the sensitivity term of each step; objective sum_t sum_{i<L} T / (L nt)."""
+    p = hst_params()
+    q, n, nt = 9, p.lx * p.ly, HST_LEVELS
+    L = lib.lat(q, p.lx, p.ly, 1)
+    ph = hs_phys(p)
+    ops_f, ops_a = HS.program_ops("forward", p), HS.program_ops("adjoint", p)
+    z = np.zeros(n)
+    f, g = np.zeros((q, n)), np.zeros((q, n))
+    lv = {0: dict(rho=np.ones(n), ux=z.copy(), uy=z.copy(), uz=z.copy(), tem=z.copy(), gi=np.zeros(n * q))}
+    lib.init(L, 0, f, lib.fields(rho=lv[0]["rho"], ux=z, uy=z, uz=z))
+    lib.init(L, 1, g, lib.fields(tem=z, ux=z, uy=z, uz=z))
+    for t in range(1, nt):
+        mac = {nm: np.zeros(n) for nm in FWD_NAMES}
+        snap = np.zeros(n * q)
+        lib.collide(L, A.AD_NATURAL, f, g, lib.fields(gsnap=snap, alpha=inp["alpha"], diffusivity=inp["kappa"], **mac),
+                    **ph, save=True)
+        lv[t] = dict(rho=mac["rho"], ux=mac["ux"], uy=mac["uy"], uz=mac["uz"], tem=mac["tem"], gi=snap)
+        lib.stream(L, f)
+        lib.stream(L, g)
+        replay(lib, L, f, g, ops_f, n, ux=mac["ux"], uy=mac["uy"], kappa=inp["kappa"])
+    fa, ga = np.zeros((q, n)), np.zeros((q, n))
+    last = lv[nt - 1]
+    lib.init(L, 2, fa, lib.fields(ux=last["ux"], uy=last["uy"], uz=z, ip=z, iux=z, iuy=z, iuz=z))
+    lib.init(L, 3, ga, lib.fields(ux=last["ux"], uy=last["uy"], uz=z, item=z, iqx=z, iqy=z, iqz=z))
+    am = {nm: np.zeros(n) for nm in ADJ_NAMES}
+    dfdss = np.zeros(n)
+    qn, mask = p.source()
+    for t in range(nt - 2, -1, -1):
+        s = lv[t]
+        igi = np.zeros(n * q)
+        lib.collide(L, A.AAD_NATURAL, fa, ga, lib.fields(gsnap=igi, alpha=inp["alpha"], diffusivity=inp["kappa"],
+                                                         rho=s["rho"], ux=s["ux"], uy=s["uy"], uz=s["uz"],
+                                                         tem=s["tem"], **am), **ph, save=True)
+        Fo = lib.fields(ux=s["ux"], uy=s["uy"], uz=s["uz"], tem=s["tem"], imx=am["imx"], imy=am["imy"], imz=am["imz"],
+                        item=am["item"], iqx=am["iqx"], iqy=am["iqy"], iqz=am["iqz"], diffusivity=inp["kappa"])
+        lib.sensitivity(L, 0, dfdss, Fo, inp["dads"], inp["dkds"], s["gi"], igi, qn, mask)
+        lib.stream(L, fa, True)
+        lib.stream(L, ga, True)
+        replay(lib, L, fa, ga, ops_a, n, ux=s["ux"], uy=s["uy"], rho=s["rho"], tem=s["tem"], kappa=inp["kappa"])
+    obj = 0.0
+    for t in range(nt):
+        for i in range(p.lx):
+            if i < p.L:
+                obj += lv[t]["tem"][i]
+    obj /= p.L * nt
+    return dict(dfdss=dfdss, objective=np.array(obj), fa=fa, ga=ga, tem_last=last["tem"])
+
+
 # ---------------------------------------------------------------------------- registry
 def all_cases():
     """name -> (make_inputs, run)."""
@@ -630,6 +702,7 @@ def all_cases():
         nm = "el_" + what
         cases[nm] = (lambda nm=nm, what=what: el_inputs(nm, what), el_run)
     cases["elsens_q9"] = (lambda: elsens_inputs("elsens_q9"), elsens_run)
+    cases["hst_q9"] = (lambda: hst_inputs("hst_q9"), hst_run)
     for nc in (1, 2, 3):
         nm = "resid_%d" % nc
         cases[nm] = (lambda nm=nm, nc=nc: resid_inputs(nm, nc), resid_run)
