@@ -16,6 +16,8 @@ buffers (2 x 245 MB) exceed the 129 MB L2, so no flush is needed between steps.
                populations, read alpha and kappa) / measured step time, vs MEASURED_PEAKS
   cpu_baseline the C restatement of the reference's scalar OpenMP path (oracle/), FP64, on
                the host cores, on a bounded number of steps of the same workload
+  transient_iter seconds of one transient heat-sink evaluation (4000 time steps forward and
+               adjoint, checkpoints every 100 steps) on the 192x192x96 FP32 lattice
   design_iter  seconds of one heat-sink design iteration (filter, forward and adjoint to residual
                1e-6, sensitivity, filtered sensitivity) on the 200x100 FP64 lattice, with the
                oracle port's time for the same step counts
@@ -183,6 +185,35 @@ def design_gpu(tol=1e-6, max_steps=100000):
     return p, s, r
 
 
+TRANSIENT_LATTICE = dict(nd=3, lx=192, ly=192, lz=96, storage="fp32", levels=4000, every=100)
+
+
+def transient_gpu():
+    """One transient heat-sink evaluation (forward from rest over 4000 time steps, the adjoint
+    swept back with a sensitivity term per step, checkpoints every 100 steps recomputed on the
+    device) on the 192x192x96 FP32 lattice, through panslbm2_gb300.transient."""
+    from panslbm2_gb300 import heatsink as HS
+    from panslbm2_gb300.transient import TransientHeatSink
+    d = TRANSIENT_LATTICE
+    p = HS.Params(d["nd"], d["lx"], d["ly"], d["lz"])
+    ss = HS.grf_design(d["nd"], d["lx"], d["ly"], d["lz"], seed=0, sigma=8.0)
+    alpha, kappa, dads, dkds = p.design_fields(ss)
+    tr = TransientHeatSink(p, d["storage"], checkpoint_every=d["every"])
+    tr.evaluate(alpha, kappa, dads, dkds, 2 * d["every"] + 2, release=False)   # warm-up: programs, step slots
+    t0 = time.perf_counter()
+    r = tr.evaluate(alpha, kappa, dads, dkds, d["levels"])
+    sec = time.perf_counter() - t0
+    tr.close()
+    n = p.lx * p.ly * p.lz
+    return {"lattice": "heatsink3d-192x192x96-fp32", "time_levels": d["levels"], "checkpoint_every": d["every"],
+            "segments": r["segments"], "seconds": round(sec, 3),
+            "phases_s": {k: round(v, 3) for k, v in r["times"].items()},
+            "forward_mlups": round(n * (d["levels"] - 1) / r["times"]["forward"] / 1e6, 1),
+            "objective": r["objective"],
+            "what": "forward from rest, adjoint swept back with one heat-source sensitivity term per time step, "
+                    "forward states recomputed from device checkpoints; no filter or MMA"}
+
+
 def design_cpu_per_step(p, budget_s=8.0):
     """Seconds per forward and per adjoint time step of the oracle port (FP64, all host cores) on
     the design lattice, from a bounded sample of steps with the drivers' every-step saves."""
@@ -251,6 +282,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-design", action="store_true", help="skip the design-iteration timing")
+    ap.add_argument("--no-transient", action="store_true", help="skip the transient-evaluation timing")
     args = ap.parse_args()
     wl = WORKLOADS[args.workload]
     if args.impl == "reference":
@@ -362,6 +394,11 @@ def main():
             di["cpu_sample"] = ("oracle port, FP64, %d host threads: %d forward and %d adjoint steps timed, scaled to the "
                                 "GPU's step counts" % (os.cpu_count() or 1, cs["forward_sample"], cs["adjoint_sample"]))
         line["design_iter"] = di
+    if rank == 0 and not args.no_transient:
+        try:
+            line["transient_iter"] = transient_gpu()
+        except Exception as e:   # reported, not fatal: the step throughput above stands on its own
+            line["transient_iter"] = {"error": str(e)[:300]}
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_port(p, alpha, kappa, ops, q)
     if rank == 0:

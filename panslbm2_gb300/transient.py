@@ -58,9 +58,10 @@ class TransientHeatSink:
             lp.store(A.STORE_FWD, t - t0)
             lp.store(A.STORE_SNAP, t - t0)
 
-    def evaluate(self, alpha, kappa, dads, dkds, nt):
+    def evaluate(self, alpha, kappa, dads, dkds, nt, release=True):
         """objective (time-averaged temperature on the heat source), its sensitivity dfdss and
-        the phase times; nt counts the time levels 0..nt-1 as the reference's loops do"""
+        the phase times; nt counts the time levels 0..nt-1 as the reference's loops do. With
+        release=False the device stores stay allocated for the next evaluation."""
         lp, n, K, nd = self.lp, self.n, self.K, self.p.nd
         zero, one = np.zeros(n), np.ones(n)
         times = {}
@@ -119,6 +120,7 @@ class TransientHeatSink:
         dfdss = lp.get_field(A.DFDS)
         acc = lp.get_field(A.ACC)
         times["adjoint"] = time.perf_counter() - t1
-        lp.store_release()
+        if release:
+            lp.store_release()
         objective = float(np.sum(acc[self.mask != 0])) / (self.p.L * nt)
         return dict(objective=objective, dfdss=dfdss, times=times, segments=nseg)

@@ -34,3 +34,21 @@ def test_transient_checkpointed_adjoint(every):
     close(tr.lp.get_populations(0), out["fa"], 1e-11)
     close(tr.lp.get_populations(1), out["ga"], 1e-11)
     tr.close()
+
+
+def test_transient_checkpoints_leave_the_result_unchanged_3d():
+    """D3Q15, FP32: recomputing the forward states from checkpoints every 3 steps gives the same
+    objective and sensitivity, bit for bit, as one segment (the recomputation is deterministic)."""
+    from panslbm2_gb300 import heatsink as HS
+    p = HS.Params(3, 8, 9, 7)
+    ss = np.clip(HS.grf_design(3, 8, 9, 7, seed=2, sigma=2.0), 0, 1)
+    alpha, kappa, dads, dkds = p.design_fields(ss)
+    res = []
+    for every in (3, 100):
+        tr = TransientHeatSink(p, "fp32", checkpoint_every=every)
+        res.append(tr.evaluate(alpha, kappa, dads, dkds, 12))
+        tr.close()
+    assert res[0]["segments"] == 4 and res[1]["segments"] == 1
+    assert res[0]["objective"] == res[1]["objective"]
+    assert np.array_equal(res[0]["dfdss"], res[1]["dfdss"])
+    assert np.all(np.isfinite(res[0]["dfdss"])) and np.any(res[0]["dfdss"] != 0)
