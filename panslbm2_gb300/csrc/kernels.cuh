@@ -145,6 +145,18 @@ __global__ void __launch_bounds__(kBlock, 4) k_interior(KArgs a) {
 // ---- boundary program replay ----------------------------------------------------------------
 // State of `node` after every op recorded before `seq_limit` (the reference applies edge
 // routines in call order; SmoothCorner* reads neighbours as they stand at that point).
+// the pull of eval_node for a node without boundary ops (slot_of < 0), inlined so f and g
+// stay in registers
+template <class L, class S, bool HG>
+__device__ __forceinline__ void pull_node(const KArgs &a, int node, int sgn, typename Store<S>::T *f,
+                                          typename Store<S>::T *g) {
+    using T = typename Store<S>::T;
+    int i, j, k;
+    coords<L>(a.geo, node, i, j, k);
+    load_node<L, S, HG>(static_cast<const S *>(a.src), a.geo, node, i, j, k, a.pull != 0, sgn,
+                        is_interior<L>(a.geo, i, j, k), f, g, T(a.ph.shift_f), T(a.ph.shift_g));
+}
+
 template <class L, class S, int D>
 __device__ __noinline__ void eval_node(const KArgs &a, int node, int seq_limit, typename Store<S>::T *f, typename Store<S>::T *g,
                           bool has_g, int sgn) {
@@ -254,8 +266,17 @@ __global__ void __launch_bounds__(128) k_snapshot(KArgs a) {
     using T = typename Store<S>::T;
     const int idx = blockIdx.x * 128 + threadIdx.x;
     if (idx >= a.geo.n) return;
+    const int sgn = kind_is_adjoint(K) ? 1 : -1;
+    if (a.slot_of[idx] < 0) {
+        // no boundary op writes this node and no smoothing reads it: eval_node would only pull it,
+        // so pull it here, into registers (eval_node's arrays live in local memory)
+        T f[L::Q], g[L::Q];
+        pull_node<L, S, true>(a, idx, sgn, f, g);
+        collide_node<L, T, K>(f, g, idx, a, false, a.snap, a.geo.np, nullptr);
+        return;
+    }
     T f[L::Q], g[L::Q];
-    eval_node<L, S, 4>(a, idx, 0x7fffffff, f, g, true, kind_is_adjoint(K) ? 1 : -1);
+    eval_node<L, S, 4>(a, idx, 0x7fffffff, f, g, true, sgn);
     collide_node<L, T, K>(f, g, idx, a, false, a.snap, a.geo.np, nullptr);
 }
 
@@ -265,9 +286,21 @@ __global__ void __launch_bounds__(128) k_stream_program(KArgs a, int has_g, int 
     using T = typename Store<S>::T;
     const int idx = blockIdx.x * 128 + threadIdx.x;
     if (idx >= a.geo.n) return;
+    const T sf = T(a.ph.shift_f), sg = T(a.ph.shift_g);
+    if (a.slot_of[idx] < 0) {
+        // pull only (as in k_snapshot): registers instead of eval_node's local-memory arrays
+        T f[L::Q], g[L::Q];
+        if (has_g) {
+            pull_node<L, S, true>(a, idx, sgn, f, g);
+            store_node<L, S, true>(static_cast<S *>(a.dst), a.geo, idx, f, g, sf, sg);
+        } else {
+            pull_node<L, S, false>(a, idx, sgn, f, g);
+            store_node<L, S, false>(static_cast<S *>(a.dst), a.geo, idx, f, g, sf, sg);
+        }
+        return;
+    }
     T f[L::Q], g[L::Q];
     eval_node<L, S, 4>(a, idx, 0x7fffffff, f, g, has_g != 0, sgn);
-    const T sf = T(a.ph.shift_f), sg = T(a.ph.shift_g);
     if (has_g) store_node<L, S, true>(static_cast<S *>(a.dst), a.geo, idx, f, g, sf, sg);
     else store_node<L, S, false>(static_cast<S *>(a.dst), a.geo, idx, f, g, sf, sg);
 }
