@@ -401,6 +401,13 @@ def main():
             line["transient_iter"] = {"error": str(e)[:300]}
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_port(p, alpha, kappa, ops, q)
+        ti = line.get("transient_iter", {})
+        if "seconds" in ti and line["cpu_baseline"].get("value"):
+            d = TRANSIENT_LATTICE
+            nodes = d["lx"] * d["ly"] * d["lz"]
+            ti["cpu_seconds_est"] = round(2 * (d["levels"] - 1) * nodes / (line["cpu_baseline"]["value"] * 1e6), 1)
+            ti["cpu_sample"] = ("the cpu_baseline step rate (oracle port, FP64, all host threads) applied to the "
+                                "forward and adjoint steps, without recomputation")
     if rank == 0:
         print(json.dumps(line), flush=True)
     lp.close()
