@@ -107,6 +107,19 @@ class Clocks:
                 "reasons": reasons, "samples": len(sm)}
 
 
+def replica_throughput(ms_local, nodes, steps, world, dist=None, device="cuda"):
+    """Whole-job throughput of `world` independent replicas (one per rank, each `nodes` nodes and
+    `steps` steps): the time is the maximum over ranks, the node updates are summed. Returns
+    (max ms, MLUPS)."""
+    tmax = float(ms_local)
+    if dist is not None and world > 1:
+        import torch
+        t = torch.tensor([tmax], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        tmax = float(t.item())
+    return tmax, world * nodes * steps / (tmax / 1e3) / 1e6
+
+
 def peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -336,13 +349,8 @@ def main():
     _, l1 = lp.stats()
     ck = clocks.stop()
     lp.synchronize()
-    tmax = ms
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        tmax = float(t.item())
+    tmax, value = replica_throughput(ms, n, args.steps, world, dist, "cuda")
     ms_step = tmax / args.steps
-    value = world * n * args.steps / (tmax / 1e3) / 1e6
 
     # end to end through the C ABI with pinned host buffers
     ha = torch.from_numpy(alpha).pin_memory()
