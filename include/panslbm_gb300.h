@@ -261,7 +261,8 @@ int pl_sensitivity(pl_lattice h, int which, double *dfds, const double *dads, co
  *   PL_STORE_POPS  both population sets of the current buffer (a checkpoint);
  *   PL_STORE_FWD   rho, ux, uy, uz, T saved by the last saving forward collide; pl_load puts them
  *                  in PL_FWD_* (the adjoint collides' and adjoint routines' forward inputs);
- *   PL_STORE_SNAP  the forward g snapshot (pl_snapshot slot 0); pl_load puts it back in slot 0. */
+ *   PL_STORE_SNAP  the forward g snapshot (pl_snapshot slot 0); pl_load puts it back in slot 0.
+ * Slots are numbered 0 .. 65535 per kind. */
 #define PL_STORE_POPS 0
 #define PL_STORE_FWD 1
 #define PL_STORE_SNAP 2

@@ -1343,6 +1343,7 @@ int pl_sensitivity_compliance(pl_lattice h, double *dfds, const double *const *i
 }
 
 // ---- checkpointed sweeps --------------------------------------------------------------------
+constexpr int kMaxStoreSlots = 1 << 16;   // per kind; a slot is a whole-lattice buffer
 static size_t store_bytes(pl_lattice h, int what) {
     if (what == PL_STORE_POPS) return (size_t)2 * h->q * h->np * h->ssize;
     if (what == PL_STORE_FWD) return sizeof(double) * 5 * (size_t)h->n;
@@ -1350,7 +1351,8 @@ static size_t store_bytes(pl_lattice h, int what) {
 }
 
 int pl_store(pl_lattice h, int what, int slot) {
-    if (!h || what < PL_STORE_POPS || what > PL_STORE_SNAP || slot < 0) return fail(PL_ERR_ARG, "bad arguments");
+    if (!h || what < PL_STORE_POPS || what > PL_STORE_SNAP || slot < 0 || slot >= kMaxStoreSlots)
+        return fail(PL_ERR_ARG, "bad arguments (slot %d of at most %d)", slot, kMaxStoreSlots);
     std::vector<void *> &v = h->store[what];
     if ((int)v.size() <= slot) v.resize(slot + 1, nullptr);
     int r;
