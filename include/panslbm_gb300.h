@@ -269,6 +269,9 @@ int pl_sensitivity(pl_lattice h, int which, double *dfds, const double *dads, co
 int pl_store(pl_lattice h, int what, int slot);
 int pl_load(pl_lattice h, int what, int slot);
 int pl_store_release(pl_lattice h);
+/* exchange the forward snapshot (slot 0) with PL_STORE_SNAP slot `slot`, without a copy: a sweep
+ * that takes each step's snapshot once and reads it back once moves it in and out this way */
+int pl_store_swap_snapshot(pl_lattice h, int slot);
 /* pl_sensitivity on the device: accumulates into the device field PL_DFDS (reset it with
  * pl_set_field, read it with pl_get_field), so a transient sweep adds one term per time step
  * (production/heatsink_transient.cpp:191-194) without host traffic. dads, dkds, qn and mask are

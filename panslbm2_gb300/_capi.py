@@ -60,7 +60,7 @@ EXPORTS = [
     "pl_set_populations", "pl_get_populations", "pl_set_field", "pl_get_field", "pl_freeze_forward",
     "pl_program_create", "pl_program_destroy", "pl_init", "pl_init_elastic", "pl_collide", "pl_step", "pl_steps", "pl_stream",
     "pl_solve", "pl_snapshot", "pl_set_snapshot", "pl_residual", "pl_residual_host", "pl_residual_device_noalloc",
-    "pl_sensitivity", "pl_sensitivity_compliance", "pl_store", "pl_load", "pl_store_release",
+    "pl_sensitivity", "pl_sensitivity_compliance", "pl_store", "pl_load", "pl_store_release", "pl_store_swap_snapshot",
     "pl_sensitivity_device", "pl_accumulate", "pl_heaviside_var",
     "pl_heaviside_sens", "pl_density_filter", "pl_normalize", "pl_stats", "pl_mma_create", "pl_mma_set_param",
     "pl_mma_update", "pl_mma_destroy", "pl_mma_get_state", "pl_mma_set_state",

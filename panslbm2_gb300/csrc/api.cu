@@ -1400,6 +1400,21 @@ int pl_load(pl_lattice h, int what, int slot) {
     return PL_OK;
 }
 
+int pl_store_swap_snapshot(pl_lattice h, int slot) {
+    if (!h || slot < 0 || slot >= kMaxStoreSlots) return fail(PL_ERR_ARG, "bad arguments (slot %d)", slot);
+    std::vector<void *> &v = h->store[PL_STORE_SNAP];
+    if ((int)v.size() <= slot) v.resize(slot + 1, nullptr);
+    int r;
+    const size_t bytes = store_bytes(h, PL_STORE_SNAP);
+    if (!v[slot] && (r = dalloc(&v[slot], bytes))) return r;
+    if (!h->snap[0] && (r = ensure_d(h, &h->snap[0], (size_t)h->q * h->np))) return r;
+    // launches already queued keep the pointers they were given; stream order does the rest
+    void *t = v[slot];
+    v[slot] = h->snap[0];
+    h->snap[0] = static_cast<double *>(t);
+    return PL_OK;
+}
+
 int pl_store_release(pl_lattice h) {
     if (!h) return fail(PL_ERR_ARG, "null handle");
     CK(cudaStreamSynchronize(h->st));

@@ -175,6 +175,9 @@ class LatticePair:
     def load(self, what, slot):
         check(self.lib.pl_load(self.h, what, slot))
 
+    def swap_snapshot(self, slot):
+        check(self.lib.pl_store_swap_snapshot(self.h, slot))
+
     def store_release(self):
         check(self.lib.pl_store_release(self.h))
 

@@ -56,7 +56,7 @@ class TransientHeatSink:
                 lp.step(A.AD_NATURAL, ph, self.prog_f, save=True)
             lp.snapshot(0, host=False)
             lp.store(A.STORE_FWD, t - t0)
-            lp.store(A.STORE_SNAP, t - t0)
+            lp.swap_snapshot(t - t0)   # moved, not copied: each snapshot is read back once
 
     def evaluate(self, alpha, kappa, dads, dkds, nt, release=True):
         """objective (time-averaged temperature on the heat source), its sensitivity dfdss and
@@ -102,7 +102,7 @@ class TransientHeatSink:
                     lp.load(A.STORE_POPS, park)
                     loaded_seg = seg
                 lp.load(A.STORE_FWD, t - (seg * K + 1))
-                lp.load(A.STORE_SNAP, t - (seg * K + 1))
+                lp.swap_snapshot(t - (seg * K + 1))
             else:
                 # time level 0: the state at rest, and no forward snapshot
                 for fid, v in ((A.FWD_RHO, one), (A.FWD_UX, zero), (A.FWD_UY, zero), (A.FWD_UZ, zero),
