@@ -16,6 +16,7 @@ buffers (2 x 245 MB) exceed the 129 MB L2, so no flush is needed between steps.
                populations, read alpha and kappa) / measured step time, vs MEASURED_PEAKS
   cpu_baseline the C restatement of the reference's scalar OpenMP path (oracle/), FP64, on
                the host cores, on a bounded number of steps of the same workload
+  design_iter_3d the same design iteration, plain method, on the 160x160x80 FP32 lattice
   transient_iter seconds of one transient heat-sink evaluation (4000 time steps forward and
                adjoint, checkpoints every 100 steps) on the 192x192x96 FP32 lattice
   design_iter  seconds of one heat-sink design iteration (filter, forward and adjoint to residual
@@ -196,6 +197,28 @@ def design_gpu(tol=1e-6, max_steps=100000):
     r = hs.iterate(s, tol=tol, max_steps=max_steps)
     hs.close()
     return p, s, r
+
+
+def design_gpu_3d(tol=1e-6, max_steps=100000):
+    """The plain design iteration on the 160x160x80 FP32 lattice (the learned warm start's
+    comparison point): filter, forward and adjoint from rest to `tol`, sensitivity."""
+    from panslbm2_gb300 import heatsink as HS
+    from panslbm2_gb300.design import HeatSinkDesign
+    p = HS.Params(3, 160, 160, 80)
+    s = HS.grf_design(3, 160, 160, 80, seed=0, sigma=8.0)
+    hs = HeatSinkDesign(p, "fp32")
+    hs.iterate(s, tol=tol, max_steps=200)          # warm-up: filter taps, programs
+    r = hs.iterate(s, tol=tol, max_steps=max_steps)
+    hs.close()
+    from panslbm2_gb300 import _capi as A
+    return {"lattice": "heatsink3d-160x160x80-fp32", "tol": tol, "max_steps": max_steps,
+            "seconds": round(r["seconds"]["total"], 3),
+            "phases_s": {k: round(v, 3) for k, v in r["seconds"].items()},
+            "forward_steps": r["forward"][1], "adjoint_steps": r["adjoint"][1],
+            "converged": [r["forward"][0] == A.PL_CONVERGED, r["adjoint"][0] == A.PL_CONVERGED],
+            "objective": r["objective"],
+            "what": "plain method from rest (no warm start): filter, forward and adjoint to the residual tolerance, "
+                    "heat-source sensitivity, filtered and normalised sensitivity"}
 
 
 TRANSIENT_LATTICE = dict(nd=3, lx=192, ly=192, lz=96, storage="fp32", levels=4000, every=100)
@@ -402,6 +425,11 @@ def main():
             di["cpu_sample"] = ("oracle port, FP64, %d host threads: %d forward and %d adjoint steps timed, scaled to the "
                                 "GPU's step counts" % (os.cpu_count() or 1, cs["forward_sample"], cs["adjoint_sample"]))
         line["design_iter"] = di
+    if rank == 0 and not args.no_design:
+        try:
+            line["design_iter_3d"] = design_gpu_3d()
+        except Exception as e:   # reported, not fatal
+            line["design_iter_3d"] = {"error": str(e)[:300]}
     if rank == 0 and not args.no_transient:
         try:
             line["transient_iter"] = transient_gpu()
