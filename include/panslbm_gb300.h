@@ -133,6 +133,13 @@ extern "C" {
 #define PL_DKDS 39
 #define PL_QN 40
 #define PL_ACC 41       /* a free accumulator for pl_accumulate                              */
+/* forced-convection heat-sink extension (no counterpart in the reference, whose heat sinks take
+ * their heat through a boundary flux): while set, PL_AD_FORCE collides add the volumetric heat
+ * source Q(x) as w_c * Q to g before their final AD macro, and PL_AAD_FORCE collides add the
+ * objective weight w(x) = dJ/dT(x) of a volumetric objective J = sum w T to every adjoint g
+ * population before a final AAD macro. pl_set_field(h, field, NULL) switches the term off. */
+#define PL_HEAT_SOURCE 42
+#define PL_OBJ_WEIGHT 43
 
 typedef struct pl_lattice_s *pl_lattice;
 
@@ -176,6 +183,10 @@ int pl_set_stream(pl_lattice h, void *stream);
 #define PL_OPT_GRAPHS 1
 #define PL_OPT_SIDE_PRIORITY 2
 int pl_set_option(pl_lattice h, int option, int value);
+/* time-varying inflow (no counterpart in the reference, whose inflows are constant): the
+ * prescribed velocity of every NS SetU / ANS iSetU op is multiplied by `scale` in the steps that
+ * follow (default 1; a transient driver sets u(t)/u_max before each step) */
+int pl_set_inflow_scale(pl_lattice h, double scale);
 /* shift of 16-bit population storage, per set (default: f 1.0, g 0.0) */
 int pl_set_shift(pl_lattice h, double shift_f, double shift_g);
 
@@ -241,8 +252,9 @@ int pl_residual_host(pl_lattice h, int n, int ncomp, const double *const *a, con
  * Residual runs on host arrays). Allocates nothing: its scratch is a fixed 16 KB device array
  * in the library, shared by all calls on a device. The first call on each device looks that
  * array up (make it before any stream capture on the device); calls from several host threads
- * that can overlap on the GPU race on it and must be serialised. Returns after the result has
- * been copied to *out. */
+ * that can overlap on the GPU race on it and must be serialised. The arrays must live on the
+ * current device (or be managed memory), else PL_ERR_ARG. Returns after the result has been
+ * copied to *out; PL_ERR_NONFINITE (with *out set) when an input value is not finite. */
 int pl_residual_device_noalloc(long long n, int ncomp, const double *const *a, const double *const *b, void *stream,
                                double *out);
 
@@ -313,6 +325,12 @@ int pl_mma_destroy(pl_mma h);
 int pl_mma_get_state(pl_mma h, int *k, double *previous, double *xkm2, double *xkm1, double *L, double *U);
 int pl_mma_set_state(pl_mma h, int k, double previous, const double *xkm2, const double *xkm1, const double *L,
                      const double *U);
+
+/* host-side fault injection (no counterpart in the reference, which has no error paths): after
+ * `after` further successful device allocations by the library, the next one fails and returns
+ * PL_ERR_ALLOC as an out-of-memory device would; -1 switches it off. For tests of callers'
+ * error handling; nothing on the device faults. */
+int pl_debug_fail_alloc(long long after);
 
 /* last step kernel time (ms) measured with CUDA events on the lattice stream, and number
  * of kernels launched since creation */

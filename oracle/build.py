@@ -2,8 +2,10 @@
 
 * ``liboracle.so``  -- the plain-C restatement (oracle.c), built with gcc on any host;
 * ``_ref/libref.so`` -- the same API bound to the PANSLBM2 reference's own header templates,
-  compiled from the reference sources where they lie (default /root/reference, override with
-  PANSLBM2_REF). Built only where those sources exist; nothing is copied from them.
+  compiled from the reference sources where they lie: the tree named by PANSLBM2_REF, or the
+  one a build step passed to ``build_ref(root=...)`` (recorded in ``_ref/REFERENCE_ROOT``).
+  Built only where those sources exist; nothing is copied from them. With neither set, the
+  reference-backed checks are skipped and say so.
 
 Both use ``-O2 -ffp-contract=off`` so that the two agree bit-for-bit on the scalar path.
 """
@@ -12,7 +14,7 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_DEFAULT = "/root/reference"
+MARKER = os.path.join(HERE, "_ref", "REFERENCE_ROOT")
 FLAGS = ["-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", "-fno-fast-math"]
 
 
@@ -32,18 +34,35 @@ def build_oracle(force=False):
     return out
 
 
+def _is_reference(root):
+    return bool(root) and os.path.isfile(os.path.join(root, "src", "particle", "d2q9.h"))
+
+
 def reference_root():
-    root = os.environ.get("PANSLBM2_REF", REF_DEFAULT)
-    return root if os.path.isfile(os.path.join(root, "src", "particle", "d2q9.h")) else None
+    """The reference tree: PANSLBM2_REF if it names one, else the tree the last build_ref(root=...)
+    recorded; None when neither exists on this machine (PANSLBM2_REF not set: the
+    reference-backed checks skip)."""
+    env = os.environ.get("PANSLBM2_REF")
+    if _is_reference(env):
+        return env
+    try:
+        with open(MARKER) as fh:
+            rec = fh.read().strip()
+    except OSError:
+        rec = None
+    return rec if _is_reference(rec) else None
 
 
-def build_ref(force=False):
-    """Compile the reference-backed library; returns its path or None when the sources are absent."""
-    root = reference_root()
+def build_ref(force=False, root=None):
+    """Compile the reference-backed library from the tree `root` (default: reference_root());
+    returns its path or None when the sources are absent."""
+    root = root if _is_reference(root) else reference_root()
     if root is None:
         return None
     outdir = os.path.join(HERE, "_ref")
     os.makedirs(outdir, exist_ok=True)
+    with open(MARKER, "w") as fh:
+        fh.write(root + "\n")
     out = os.path.join(outdir, "libref.so")
     srcs = [os.path.join(HERE, f) for f in ("ref_harness.cpp", "ref_api.cpp", "oracle.h")]
     if not force and _newer(out, srcs):
@@ -59,10 +78,10 @@ def build_ref(force=False):
     return out
 
 
-def build_ref_mma(force=False):
+def build_ref_mma(force=False, root=None):
     """The reference's own MMA<double> behind a C entry point (golden vectors of the MMA update);
     None when the reference sources are absent."""
-    root = reference_root()
+    root = root if _is_reference(root) else reference_root()
     if root is None:
         return None
     outdir = os.path.join(HERE, "_ref")
@@ -76,4 +95,4 @@ def build_ref_mma(force=False):
 
 if __name__ == "__main__":
     print(build_oracle(force="-f" in sys.argv))
-    print(build_ref(force="-f" in sys.argv))
+    print(build_ref(force="-f" in sys.argv, root=sys.argv[-1] if len(sys.argv) > 1 else None))

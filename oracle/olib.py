@@ -33,7 +33,7 @@ class Lat(C.Structure):
 FIELD_NAMES = ["rho", "ux", "uy", "uz", "tem", "qx", "qy", "qz", "ip", "iux", "iuy", "iuz",
                "imx", "imy", "imz", "item", "iqx", "iqy", "iqz", "alpha", "diffusivity", "beta",
                "dirx", "diry", "dirz", "gsnap", "sxx", "sxy", "syx", "syy", "isxx", "isxy", "isyx", "isyy",
-               "gamma"]
+               "gamma", "hsrc", "objw"]
 
 
 class Fields(C.Structure):
@@ -48,7 +48,8 @@ class Phys(C.Structure):
 class BC(C.Structure):
     _fields_ = [("kind", C.c_int), ("axis", C.c_int), ("pos", C.c_int), ("dir", C.c_int), ("type", IP),
                 ("v0", DP), ("v1", DP), ("v2", DP), ("ux", DP), ("uy", DP), ("uz", DP), ("rho", DP),
-                ("tem", DP), ("diffusivity", DP), ("kappa", C.c_double), ("eps", C.c_double)]
+                ("tem", DP), ("diffusivity", DP), ("kappa", C.c_double), ("eps", C.c_double),
+                ("uscale", C.c_double)]
 
 
 def _dp(a):
@@ -111,9 +112,9 @@ class Oracle:
         self.lib.ol_stream(C.byref(L), _dp(f), int(inverse))
 
     def apply_bc(self, L, f, kind, axis, pos, dir, type, g=None, v0=None, v1=None, v2=None, ux=None, uy=None,
-                 uz=None, rho=None, tem=None, diffusivity=None, kappa=0.0, eps=0.0):
+                 uz=None, rho=None, tem=None, diffusivity=None, kappa=0.0, eps=0.0, uscale=1.0):
         b = BC(kind, axis, pos, dir, _ip(type), _dp(v0), _dp(v1), _dp(v2), _dp(ux), _dp(uy), _dp(uz), _dp(rho),
-               _dp(tem), _dp(diffusivity), float(kappa), float(eps))
+               _dp(tem), _dp(diffusivity), float(kappa), float(eps), float(uscale))
         self.lib.ol_apply_bc(C.byref(L), _dp(f), _dp(g), C.byref(b))
 
     def smooth_corner(self, L, f):

@@ -169,7 +169,8 @@ static void zouhe_node(const lat_t *t, int idx, int i, int j, int k, void *vctx)
     }
     double S = sT + 2.0 * sO;
     if (bc->kind == OL_BC_NS_U) {
-        u[0] = bc->v0[idx]; u[1] = bc->v1[idx]; if (nd == 3) u[2] = bc->v2[idx];
+        /* uscale: time-varying inflow (CPU extension; 1 = the reference routine) */
+        u[0] = bc->uscale * bc->v0[idx]; u[1] = bc->uscale * bc->v1[idx]; if (nd == 3) u[2] = bc->uscale * bc->v2[idx];
         rho0 = S / (d < 0 ? 1.0 - u[a] : 1.0 + u[a]);
     } else {
         /* SetRho: v0 = rho, v1 = first tangential (cyclic), v2 = second tangential */
@@ -310,7 +311,7 @@ static void ans_node(const lat_t *t, int idx, int i, int j, int k, void *vctx) {
         for (int c = 1; c < t->q; ++c) if (t->c[a][c] == d) F(f, c, idx) = F(f, opp_of(t, c), idx) - rho0;
         return;
     }
-    double u[3] = {bc->v0[idx], bc->v1[idx], nd == 3 ? bc->v2[idx] : 0.0};
+    double u[3] = {bc->uscale * bc->v0[idx], bc->uscale * bc->v1[idx], nd == 3 ? bc->uscale * bc->v2[idx] : 0.0};
     if (nd == 2) {
         double un = u[0], ut = (a == 0) ? u[1] : u[0];  /* y edges use ux twice (reference) */
         int b = 1 - a;
@@ -688,6 +689,11 @@ static void ad_heatex(const lat_t *t, double *g, double tem, double beta) {
     g[0] += t->w[0] * coef;
     for (int c = 1; c < t->q; ++c) g[c] += t->w[c] * coef;
 }
+/* Volumetric heat source (CPU extension, no reference routine; parity unpinned): g_c += w_c Q,
+ * the same form as the heat-exchange term above with a fixed source Q */
+static void ad_source(const lat_t *t, double *g, double qsrc) {
+    for (int c = 0; c < t->q; ++c) g[c] += t->w[c] * qsrc;
+}
 /* ANS::Macro (adjointnavierstokes.h:15-57) */
 static void ans_macro(const lat_t *t, const double *f, const double *u, double *ip, double *iu, double *im) {
     double uu = vdot(t, u, u);
@@ -760,6 +766,12 @@ static void aad_heatex(const lat_t *t, double *g, double item, double beta) {
     double coef = beta * (1.0 + item) / (1.0 + beta);
     g[0] -= coef;
     for (int c = 1; c < t->q; ++c) g[c] -= coef;
+}
+/* adjoint source of a volumetric objective J = sum_x w(x) T(x) (CPU extension, parity unpinned):
+ * dJ/dg_c = w for every c, added in the convention of AAD::ExternalForceHeatExchange above,
+ * whose "1" term is the derivative of its heat-exchange objective */
+static void aad_objective_source(const lat_t *t, double *g, double w) {
+    for (int c = 0; c < t->q; ++c) g[c] += w;
 }
 /* AAD::ExternalForceNaturalConvection (adjointadvection.h:114-132) */
 static void aad_nc(const lat_t *t, double *g, const double *im, const double *gv) {
@@ -968,6 +980,7 @@ void ol_collide(const ol_lat *L, int kind, double *fa, double *ga, const ol_fiel
                 ns_brinkman(t, f, rho, u, Fd->alpha[idx]);
                 ns_macro(t, f, &rho, u);
                 if (kind == OL_AD_HEATEX) ad_heatex(t, g, tem, Fd->beta[idx]);
+                if (kind == OL_AD_FORCE && Fd->hsrc) ad_source(t, g, Fd->hsrc[idx]);
                 if (ga) ad_macro(t, g, u, omg, &tem, qv);
             } else if (kind == OL_AD_NATURAL) {
                 ad_nc_force(t, f, tem, gv, P->tem0);
@@ -1012,6 +1025,9 @@ void ol_collide(const ol_lat *L, int kind, double *fa, double *ga, const ol_fiel
                     aad_macro(t, g, &item, iq);
                 } else if (kind == OL_AAD_HEATEX) {
                     aad_heatex(t, g, item, Fd->beta[idx]);
+                    aad_macro(t, g, &item, iq);
+                } else if (kind == OL_AAD_FORCE && Fd->objw) {
+                    aad_objective_source(t, g, Fd->objw[idx]);
                     aad_macro(t, g, &item, iq);
                 }
             }

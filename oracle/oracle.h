@@ -42,6 +42,13 @@ typedef struct {
     double *sxx, *sxy, *syx, *syy;
     double *isxx, *isxy, *isyx, *isyy;
     const double *gamma;                        /* stress scale gamma[N] (EL extended, AEL)    */
+    /* CPU extension for the forced-convection heat-sink configurations (no reference routine;
+     * parity vs the reference unpinned, this restatement is the oracle): with OL_AD_FORCE,
+     * hsrc[idx] is a volumetric heat source added as w_c * hsrc to g before the final AD macro;
+     * with OL_AAD_FORCE, objw[idx] = dJ/dT of a volumetric objective J = sum objw * T, added to
+     * every adjoint g population before a final AAD macro. NULL = off (the reference routine). */
+    const double *hsrc;
+    const double *objw;
 } ol_fields;
 
 typedef struct {
@@ -108,6 +115,9 @@ typedef struct {
     const double *diffusivity;    /* per-node kappa (OL_BC_AD_Q)                  */
     double kappa;                 /* constant kappa (OL_BC_AD_QC)                 */
     double eps;                   /* objective weight of adjoint BCs              */
+    double uscale;                /* factor on the prescribed velocity of NS SetU / ANS iSetU
+                                   * (time-varying inflow u(t) = uscale * u; CPU extension,
+                                   * 1 = the reference routine)                    */
 } ol_bc;
 
 /* lattice geometry ------------------------------------------------------- */

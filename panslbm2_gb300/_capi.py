@@ -33,6 +33,7 @@ RHO, UX, UY, UZ, TEM, QX, QY, QZ = 8, 9, 10, 11, 12, 13, 14, 15
 IP, IUX, IUY, IUZ, IMX, IMY, IMZ, ITEM, IQX, IQY, IQZ = 16, 17, 18, 19, 20, 21, 22, 23, 24, 25, 26
 FWD_RHO, FWD_UX, FWD_UY, FWD_UZ, FWD_TEM = 32, 33, 34, 35, 36
 DFDS, DADS, DKDS, QN, ACC = 37, 38, 39, 40, 41
+HEAT_SOURCE, OBJ_WEIGHT = 42, 43
 STORE_POPS, STORE_FWD, STORE_SNAP = 0, 1, 2
 # the elastic kinds' macros share the planes above
 SXX, SXY, SYX, SYY = TEM, QX, QY, QZ
@@ -56,14 +57,14 @@ class BcDesc(C.Structure):
 
 EXPORTS = [
     "pl_create", "pl_destroy", "pl_last_error", "pl_synchronize", "pl_set_stream", "pl_set_option",
-    "pl_set_shift",
+    "pl_set_shift", "pl_set_inflow_scale",
     "pl_set_populations", "pl_get_populations", "pl_set_field", "pl_get_field", "pl_freeze_forward",
     "pl_program_create", "pl_program_destroy", "pl_init", "pl_init_elastic", "pl_collide", "pl_step", "pl_steps", "pl_stream",
     "pl_solve", "pl_snapshot", "pl_set_snapshot", "pl_residual", "pl_residual_host", "pl_residual_device_noalloc",
     "pl_sensitivity", "pl_sensitivity_compliance", "pl_store", "pl_load", "pl_store_release", "pl_store_swap_snapshot",
     "pl_sensitivity_device", "pl_accumulate", "pl_heaviside_var",
     "pl_heaviside_sens", "pl_density_filter", "pl_normalize", "pl_stats", "pl_mma_create", "pl_mma_set_param",
-    "pl_mma_update", "pl_mma_destroy", "pl_mma_get_state", "pl_mma_set_state",
+    "pl_mma_update", "pl_mma_destroy", "pl_mma_get_state", "pl_mma_set_state", "pl_debug_fail_alloc",
 ]
 
 _lib = None

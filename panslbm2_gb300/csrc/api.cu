@@ -7,10 +7,13 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <map>
 #include <string>
 #include <vector>
+
+#include <nvtx3/nvToolsExt.h>
 
 #include "../../include/panslbm_gb300.h"
 #include "common.h"
@@ -23,6 +26,13 @@ using pl::Op;
 namespace {
 
 thread_local std::string g_err;
+
+// NVTX range around a C-ABI call (visible in Nsight timelines; no cost without a profiler)
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+};
+#define PL_RANGE(name) NvtxRange nvtx_range_(name)
 
 int fail(int code, const char *fmt, ...) {
     char buf[512];
@@ -83,8 +93,8 @@ struct pl_lattice_s {
     int cur = 0;
     double shift_f = 1.0, shift_g = 0.0;
     double *fld[48] = {nullptr};     // double fields by PL_* id (design inputs, forward solution)
-    void *cfld[13] = {nullptr};      // compute-type copies: alpha,kappa,beta,dirx,diry,dirz,frho,fux,fuy,fuz,ftem,
-                                     // EL density, gamma
+    void *cfld[15] = {nullptr};      // compute-type copies: alpha,kappa,beta,dirx,diry,dirz,frho,fux,fuy,fuz,ftem,
+                                     // EL density, gamma, heat source, objective weight
     double *fwd[2][8] = {{nullptr}};
     double *adj[2][11] = {{nullptr}};
     int fwd_next = 0, adj_next = 0;  // slot the next collide writes
@@ -92,6 +102,7 @@ struct pl_lattice_s {
     int fwd_latest = -1;             // slot written by the last forward collide (boundary u)
     std::vector<Program> progs;
     double *snap[2] = {nullptr, nullptr};
+    bool snap_ok[2] = {false, false};   // the snapshot buffer holds a taken / loaded snapshot
     // last collide, for snapshots
     int last_kind = -1, last_src = -1, last_prog = -1, last_pull = 0, last_bcu_slot = -1;
     pl_phys last_ph{};
@@ -114,6 +125,8 @@ struct pl_lattice_s {
     struct GraphKey {
         int kind, prog, cur, fwd_next, adj_next, fwd_latest;
         pl_phys ph;
+        const void *hsrc, *objw;   // source fields in use (their pointers are baked into the graph)
+        double uscale;
         bool operator<(const GraphKey &o) const { return memcmp(this, &o, sizeof *this) < 0; }
     };
     struct GraphEntry { cudaGraphExec_t exec; long long launches; };
@@ -122,7 +135,9 @@ struct pl_lattice_s {
     bool use_graphs = true;
     // device stores of a checkpointed sweep, per kind (populations, forward macros, snapshot)
     std::vector<void *> store[3];
+    std::vector<char> snap_filled;   // PL_STORE_SNAP slots that hold a snapshot
     int *sens_mask = nullptr;        // source mask of pl_sensitivity_device
+    double uscale = 1.0;             // pl_set_inflow_scale
 };
 
 namespace {
@@ -136,7 +151,17 @@ AuxFn pick_aux(int q, int s) {
     return s == PL_FP64 ? pl::aux_d3q15_f64 : s == PL_FP32 ? pl::aux_d3q15_f32 : s == PL_FP16 ? pl::aux_d3q15_f16 : pl::aux_d3q15_bf16;
 }
 
+// host-side fault injection for tests (pl_debug_fail_alloc): after this many more successful
+// device allocations the next one fails as if the device were out of memory; -1 = off
+std::atomic<long long> g_fail_alloc_after{-1};
+
 int dalloc(void **p, size_t bytes) {
+    long long left = g_fail_alloc_after.load();
+    while (left >= 0 && !g_fail_alloc_after.compare_exchange_weak(left, left - 1)) {}
+    if (left == 0) {
+        *p = nullptr;
+        return fail(PL_ERR_ALLOC, "cudaMalloc(%zu): injected allocation failure", bytes);
+    }
     cudaError_t e = cudaMalloc(p, bytes);
     if (e != cudaSuccess) { *p = nullptr; cudaGetLastError(); return fail(PL_ERR_ALLOC, "cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e)); }
     return PL_OK;
@@ -169,6 +194,7 @@ int field_index_c(int f) {
     if (f >= PL_ALPHA && f <= PL_DIRZ) return f;
     if (f >= PL_FWD_RHO && f <= PL_FWD_TEM) return 6 + (f - PL_FWD_RHO);
     if (f == PL_DENSITY || f == PL_GAMMA) return 11 + (f - PL_DENSITY);
+    if (f == PL_HEAT_SOURCE || f == PL_OBJ_WEIGHT) return 13 + (f - PL_HEAT_SOURCE);
     return -1;
 }
 // make sure a compute-type copy of field f exists and is current
@@ -543,6 +569,7 @@ int build_args(pl_lattice h, int kind, const pl_phys *ph, int prog, int src, int
     a.pull = pull ? 1 : 0;
     a.save = save ? 1 : 0;
     a.err = h->err;
+    a.uscale = h->uscale;
     const bool adjk = pl::kind_is_adjoint(kind);
     const bool elk = pl::kind_elastic(kind);
     a.sgn = adjk ? 1 : -1;
@@ -576,6 +603,14 @@ int build_args(pl_lattice h, int kind, const pl_phys *ph, int prog, int src, int
         if (!h->fld[PL_BETA]) return fail(PL_ERR_STATE, "kind %d needs PL_BETA", kind);
         if ((r = ensure_cfield(h, PL_BETA))) return r;
         a.beta = h->cfld[2];
+    }
+    if (kind == PL_AD_FORCE && h->fld[PL_HEAT_SOURCE]) {
+        if ((r = ensure_cfield(h, PL_HEAT_SOURCE))) return r;
+        a.hsrc = h->cfld[13];
+    }
+    if (kind == PL_AAD_FORCE && h->fld[PL_OBJ_WEIGHT]) {
+        if ((r = ensure_cfield(h, PL_OBJ_WEIGHT))) return r;
+        a.objw = h->cfld[14];
     }
     if (kind == PL_AAD_MASSFLOW) {
         for (int f = PL_DIRX; f <= (h->nd == 3 ? PL_DIRZ : PL_DIRY); ++f) {
@@ -741,13 +776,23 @@ Taps *get_taps(pl_lattice h, double R) {
             }
     Taps t;
     t.ntap = (int)di.size();
+    auto release = [&t]() {
+        cudaFree(t.di); cudaFree(t.dj); cudaFree(t.dk); cudaFree(t.hat);
+        return (Taps *)nullptr;
+    };
     if (dalloc((void **)&t.di, sizeof(int) * t.ntap) || dalloc((void **)&t.dj, sizeof(int) * t.ntap) ||
         dalloc((void **)&t.dk, sizeof(int) * t.ntap) || dalloc((void **)&t.hat, sizeof(double) * t.ntap))
-        return nullptr;
-    cudaMemcpy(t.di, di.data(), sizeof(int) * t.ntap, cudaMemcpyHostToDevice);
-    cudaMemcpy(t.dj, dj.data(), sizeof(int) * t.ntap, cudaMemcpyHostToDevice);
-    cudaMemcpy(t.dk, dk.data(), sizeof(int) * t.ntap, cudaMemcpyHostToDevice);
-    cudaMemcpy(t.hat, hat.data(), sizeof(double) * t.ntap, cudaMemcpyHostToDevice);
+        return release();
+    const cudaError_t e[4] = {
+        cudaMemcpy(t.di, di.data(), sizeof(int) * t.ntap, cudaMemcpyHostToDevice),
+        cudaMemcpy(t.dj, dj.data(), sizeof(int) * t.ntap, cudaMemcpyHostToDevice),
+        cudaMemcpy(t.dk, dk.data(), sizeof(int) * t.ntap, cudaMemcpyHostToDevice),
+        cudaMemcpy(t.hat, hat.data(), sizeof(double) * t.ntap, cudaMemcpyHostToDevice)};
+    for (cudaError_t x : e)
+        if (x != cudaSuccess) {
+            fail(PL_ERR_CUDA, "filter taps upload: %s", cudaGetErrorString(x));
+            return release();
+        }
     return &(h->taps[{h->nd, key}] = t);
 }
 
@@ -765,6 +810,11 @@ int pl::record_error(int code, const char *msg) { return fail(code, "%s", msg); 
 extern "C" {
 
 const char *pl_last_error(void) { return g_err.c_str(); }
+
+int pl_debug_fail_alloc(long long after) {
+    g_fail_alloc_after.store(after < 0 ? -1 : after);
+    return PL_OK;
+}
 
 int pl_create(int q, int nx, int ny, int nz, int storage, pl_lattice *out) {
     if (!out) return fail(PL_ERR_ARG, "out is NULL");
@@ -897,6 +947,12 @@ int pl_set_option(pl_lattice h, int option, int value) {
     return fail(PL_ERR_ARG, "unknown option");
 }
 
+int pl_set_inflow_scale(pl_lattice h, double s) {
+    if (!h || !std::isfinite(s)) return fail(PL_ERR_ARG, "bad arguments");
+    h->uscale = s;
+    return PL_OK;
+}
+
 int pl_set_shift(pl_lattice h, double sf, double sg) {
     if (!h) return fail(PL_ERR_ARG, "null handle");
     h->shift_f = sf;
@@ -931,9 +987,25 @@ int pl_get_populations(pl_lattice h, int set, double *host) {
 }
 
 int pl_set_field(pl_lattice h, int f, const double *host) {
+    PL_RANGE("pl_set_field");
+    if (h && !host && (f == PL_HEAT_SOURCE || f == PL_OBJ_WEIGHT)) {
+        // switch the source term off: queued launches keep their pointers, so free in order
+        CK(cudaStreamSynchronize(h->st));
+        const int ci = field_index_c(f);
+        cudaFree(h->fld[f]); h->fld[f] = nullptr;
+        cudaFree(h->cfld[ci]); h->cfld[ci] = nullptr;
+        return PL_OK;
+    }
     if (!h || !host) return fail(PL_ERR_ARG, "bad arguments");
     int r;
-    if ((f >= PL_ALPHA && f <= PL_GAMMA) || (f >= PL_FWD_RHO && f <= PL_ACC)) {
+    if ((f >= PL_ALPHA && f <= PL_GAMMA) || (f >= PL_FWD_RHO && f <= PL_OBJ_WEIGHT)) {
+        if (f == PL_KAPPA) {
+            // a diffusivity <= 0 gives a relaxation rate 1/(3 kappa + 1/2) >= 2: the AD collide
+            // is then unstable, so refuse it before it reaches the device
+            for (int i = 0; i < h->n; ++i)
+                if (!(host[i] > 0.0) || !std::isfinite(host[i]))
+                    return fail(PL_ERR_ARG, "PL_KAPPA[%d] = %g: the diffusivity must be finite and > 0", i, host[i]);
+        }
         if ((r = ensure_d(h, &h->fld[f], h->n))) return r;
         if ((r = upload(h, h->fld[f], host, h->n))) return r;
         return sync_cfield(h, f);
@@ -954,9 +1026,10 @@ int pl_set_field(pl_lattice h, int f, const double *host) {
 }
 
 int pl_get_field(pl_lattice h, int f, double *host) {
+    PL_RANGE("pl_get_field");
     if (!h || !host) return fail(PL_ERR_ARG, "bad arguments");
     const double *src = nullptr;
-    if ((f >= PL_ALPHA && f <= PL_GAMMA) || (f >= PL_FWD_RHO && f <= PL_ACC)) src = h->fld[f];
+    if ((f >= PL_ALPHA && f <= PL_GAMMA) || (f >= PL_FWD_RHO && f <= PL_OBJ_WEIGHT)) src = h->fld[f];
     else if (f >= PL_RHO && f <= PL_QZ) src = h->fwd_saved >= 0 ? h->fwd[h->fwd_saved][f - PL_RHO] : nullptr;
     else if (f >= PL_IP && f <= PL_IQZ) src = h->adj_saved >= 0 ? h->adj[h->adj_saved][f - PL_IP] : nullptr;
     else return fail(PL_ERR_ARG, "unknown field %d", f);
@@ -981,6 +1054,7 @@ int pl_freeze_forward(pl_lattice h) {
 }
 
 int pl_program_create(pl_lattice h, const pl_bc_desc *descs, int n, int *prog) {
+    PL_RANGE("pl_program_create");
     if (!h || (!descs && n) || !prog) return fail(PL_ERR_ARG, "bad arguments");
     Program P;
     int r = compile_program(h, descs, n, P);
@@ -1003,6 +1077,7 @@ int pl_program_destroy(pl_lattice h, int prog) {
 
 int pl_init(pl_lattice h, int which, const double *a0, const double *a1, const double *a2, const double *a3,
             const double *ux, const double *uy, const double *uz) {
+    PL_RANGE("pl_init");
     if (!h || which < 0 || which > 5 || !a0) return fail(PL_ERR_ARG, "bad arguments");
     if (which >= 4 && h->nd != 2) return fail(PL_ERR_UNSUPPORTED, "init %d is D2Q9 only", which);
     if (which != 5 && (!ux || !uy || (h->nd == 3 && !uz))) return fail(PL_ERR_ARG, "init %d needs the velocity", which);
@@ -1059,16 +1134,19 @@ int pl_init_elastic(pl_lattice h, int which, const double *const *in) {
 }
 
 int pl_collide(pl_lattice h, int kind, const pl_phys *ph, int save) {
+    PL_RANGE("pl_collide");
     if (!h || !ph) return fail(PL_ERR_ARG, "bad arguments");
     return do_collide(h, kind, ph, save != 0);
 }
 
 int pl_step(pl_lattice h, int kind, const pl_phys *ph, int prog, int save) {
+    PL_RANGE("pl_step");
     if (!h || !ph) return fail(PL_ERR_ARG, "bad arguments");
     return do_step(h, kind, ph, prog, save != 0);
 }
 
 int pl_steps(pl_lattice h, int kind, const pl_phys *ph, int prog, int n) {
+    PL_RANGE("pl_steps");
     if (!h || !ph || n < 0) return fail(PL_ERR_ARG, "bad arguments");
     CK(cudaEventRecord(h->ev0, h->st));
     int r;
@@ -1082,6 +1160,9 @@ int pl_steps(pl_lattice h, int kind, const pl_phys *ph, int prog, int n) {
         pl_lattice_s::GraphKey key;
         memset(&key, 0, sizeof key);
         key.kind = kind; key.prog = prog; key.ph = *ph;
+        key.hsrc = kind == PL_AD_FORCE ? h->fld[PL_HEAT_SOURCE] : nullptr;
+        key.objw = kind == PL_AAD_FORCE ? h->fld[PL_OBJ_WEIGHT] : nullptr;
+        key.uscale = h->uscale;
         for (int warm = 0; warm < 2; ++warm) {   // settle allocations and parity before capture
             key.cur = h->cur; key.fwd_next = h->fwd_next; key.adj_next = h->adj_next; key.fwd_latest = h->fwd_latest;
             if (h->graphs.count(key)) break;
@@ -1144,6 +1225,7 @@ int pl_steps(pl_lattice h, int kind, const pl_phys *ph, int prog, int n) {
 }
 
 int pl_stream(pl_lattice h, int mode, int prog, int both_sets) {
+    PL_RANGE("pl_stream");
     if (!h || mode < 0 || mode > 3) return fail(PL_ERR_ARG, "bad arguments");
     const bool inverse = mode == 1, nopull = mode >= 2, adjin = mode == 1 || mode == 3;
     KArgs a;
@@ -1159,6 +1241,7 @@ int pl_stream(pl_lattice h, int mode, int prog, int both_sets) {
 
 int pl_solve(pl_lattice h, int kind, const pl_phys *ph, int prog, int max_steps, int check_every, double tol,
              int *status, int *steps, double *res) {
+    PL_RANGE("pl_solve");
     if (!h || !ph || max_steps < 1 || check_every < 1 || !status || !steps) return fail(PL_ERR_ARG, "bad arguments");
     const bool adjk = pl::kind_is_adjoint(kind);
     const int fa = adjk ? 2 : 0, fb = adjk ? 3 : 1;
@@ -1206,6 +1289,7 @@ int pl_solve(pl_lattice h, int kind, const pl_phys *ph, int prog, int max_steps,
 }
 
 int pl_snapshot(pl_lattice h, int slot, double *host) {
+    PL_RANGE("pl_snapshot");
     if (!h || (slot != 0 && slot != 1)) return fail(PL_ERR_ARG, "bad arguments");
     if (h->last_kind < 0) return fail(PL_ERR_STATE, "no collide to take a snapshot of");
     if (pl::kind_is_adjoint(h->last_kind) != (slot == 1)) return fail(PL_ERR_STATE, "last collide does not match slot %d", slot);
@@ -1223,6 +1307,7 @@ int pl_snapshot(pl_lattice h, int slot, double *host) {
     a.snap = h->snap[slot];
     if (h->launch(h->last_kind, pl::OP_SNAPSHOT, false, a, h->st)) return fail(PL_ERR_UNSUPPORTED, "snapshot kind");
     if ((r = check_launch(h, 1))) return r;
+    h->snap_ok[slot] = true;
     if (host) {
         double *buf;
         if ((r = scratch(h, 2, &buf))) return r;
@@ -1241,10 +1326,12 @@ int pl_set_snapshot(pl_lattice h, int slot, const double *host) {
     if ((r = scratch(h, 2, &buf))) return r;
     if ((r = upload(h, buf, host, (size_t)h->q * h->n))) return r;
     pl::launch_node_major_to_snap(buf, h->np, h->n, h->q, h->snap[slot], h->st);
+    h->snap_ok[slot] = true;
     return check_launch(h, 1);
 }
 
 int pl_residual(pl_lattice h, int family, double *out) {
+    PL_RANGE("pl_residual");
     if (!h || !out || family < 0 || family > 3) return fail(PL_ERR_ARG, "bad arguments");
     double o[3];
     int r = residual_family(h, family, o, true);
@@ -1254,6 +1341,7 @@ int pl_residual(pl_lattice h, int family, double *out) {
 }
 
 int pl_residual_host(pl_lattice h, int n, int ncomp, const double *const *a, const double *const *b, double *out) {
+    PL_RANGE("pl_residual_host");
     if (!h || !a || !b || !out || ncomp < 1 || ncomp > 3 || n < 1 || n > h->n * h->q / 6) return fail(PL_ERR_ARG, "bad arguments");
     double *buf;
     int r = scratch(h, 3, &buf);
@@ -1279,10 +1367,11 @@ int pl_residual_host(pl_lattice h, int n, int ncomp, const double *const *a, con
 
 int pl_sensitivity(pl_lattice h, int which, double *dfds, const double *dads, const double *dkds, const double *qn,
                    const int *mask) {
+    PL_RANGE("pl_sensitivity");
     if (!h || !dfds || !dads || which < 0 || which > 3) return fail(PL_ERR_ARG, "bad arguments");
     if ((which <= 2 && !dkds) || (which == 0 && (!qn || !mask))) return fail(PL_ERR_ARG, "missing dkds / qn / mask");
     if (h->adj_saved < 0) return fail(PL_ERR_STATE, "no saved adjoint collide");
-    if (which <= 1 && (!h->snap[0] || !h->snap[1])) return fail(PL_ERR_STATE, "take both snapshots (pl_snapshot) first");
+    if (which <= 1 && (!h->snap_ok[0] || !h->snap_ok[1])) return fail(PL_ERR_STATE, "take both snapshots (pl_snapshot) first");
     for (int f = PL_FWD_RHO; f <= PL_FWD_TEM; ++f)
         if (!h->fld[f]) return fail(PL_ERR_STATE, "forward solution not set (pl_freeze_forward)");
     double *buf;
@@ -1351,6 +1440,7 @@ static size_t store_bytes(pl_lattice h, int what) {
 }
 
 int pl_store(pl_lattice h, int what, int slot) {
+    PL_RANGE("pl_store");
     if (!h || what < PL_STORE_POPS || what > PL_STORE_SNAP || slot < 0 || slot >= kMaxStoreSlots)
         return fail(PL_ERR_ARG, "bad arguments (slot %d of at most %d)", slot, kMaxStoreSlots);
     std::vector<void *> &v = h->store[what];
@@ -1370,16 +1460,21 @@ int pl_store(pl_lattice h, int what, int slot) {
             else { CK(cudaMemsetAsync(d, 0, sizeof(double) * h->n, h->st)); }
         }
     } else {
-        if (!h->snap[0]) return fail(PL_ERR_STATE, "no forward snapshot (pl_snapshot slot 0)");
+        if (!h->snap_ok[0]) return fail(PL_ERR_STATE, "no forward snapshot (pl_snapshot slot 0)");
         CK(cudaMemcpyAsync(dst, h->snap[0], bytes, cudaMemcpyDeviceToDevice, h->st));
+        if ((int)h->snap_filled.size() <= slot) h->snap_filled.resize(slot + 1, 0);
+        h->snap_filled[slot] = 1;
     }
     return PL_OK;
 }
 
 int pl_load(pl_lattice h, int what, int slot) {
+    PL_RANGE("pl_load");
     if (!h || what < PL_STORE_POPS || what > PL_STORE_SNAP || slot < 0) return fail(PL_ERR_ARG, "bad arguments");
     const std::vector<void *> &v = h->store[what];
-    if ((int)v.size() <= slot || !v[slot]) return fail(PL_ERR_STATE, "store %d slot %d is empty", what, slot);
+    if ((int)v.size() <= slot || !v[slot] ||
+        (what == PL_STORE_SNAP && ((int)h->snap_filled.size() <= slot || !h->snap_filled[slot])))
+        return fail(PL_ERR_STATE, "store %d slot %d is empty", what, slot);
     const char *src = static_cast<const char *>(v[slot]);
     int r;
     if (what == PL_STORE_POPS) {
@@ -1396,6 +1491,7 @@ int pl_load(pl_lattice h, int what, int slot) {
     } else {
         if ((r = ensure_d(h, &h->snap[0], (size_t)h->q * h->np))) return r;
         CK(cudaMemcpyAsync(h->snap[0], src, store_bytes(h, what), cudaMemcpyDeviceToDevice, h->st));
+        h->snap_ok[0] = true;
     }
     return PL_OK;
 }
@@ -1408,10 +1504,16 @@ int pl_store_swap_snapshot(pl_lattice h, int slot) {
     const size_t bytes = store_bytes(h, PL_STORE_SNAP);
     if (!v[slot] && (r = dalloc(&v[slot], bytes))) return r;
     if (!h->snap[0] && (r = ensure_d(h, &h->snap[0], (size_t)h->q * h->np))) return r;
-    // launches already queued keep the pointers they were given; stream order does the rest
+    // launches already queued keep the pointers they were given; stream order does the rest.
+    // An empty slot may take the current snapshot, but the snapshot buffer then holds nothing a
+    // sensitivity may read until the next pl_snapshot / pl_load / swap of a filled slot.
+    if ((int)h->snap_filled.size() <= slot) h->snap_filled.resize(slot + 1, 0);
     void *t = v[slot];
     v[slot] = h->snap[0];
     h->snap[0] = static_cast<double *>(t);
+    const bool was_ok = h->snap_ok[0];
+    h->snap_ok[0] = h->snap_filled[slot] != 0;
+    h->snap_filled[slot] = was_ok ? 1 : 0;
     return PL_OK;
 }
 
@@ -1419,14 +1521,16 @@ int pl_store_release(pl_lattice h) {
     if (!h) return fail(PL_ERR_ARG, "null handle");
     CK(cudaStreamSynchronize(h->st));
     for (auto &v : h->store) { for (void *p : v) cudaFree(p); v.clear(); }
+    h->snap_filled.clear();
     return PL_OK;
 }
 
 int pl_sensitivity_device(pl_lattice h, int which, const double *dads, const double *dkds, const double *qn,
                           const int *mask) {
+    PL_RANGE("pl_sensitivity_device");
     if (!h || which < 0 || which > 3) return fail(PL_ERR_ARG, "bad arguments");
     if (h->adj_saved < 0) return fail(PL_ERR_STATE, "no saved adjoint collide");
-    if (which <= 1 && (!h->snap[0] || !h->snap[1])) return fail(PL_ERR_STATE, "take both snapshots (pl_snapshot) first");
+    if (which <= 1 && (!h->snap_ok[0] || !h->snap_ok[1])) return fail(PL_ERR_STATE, "take both snapshots (pl_snapshot) first");
     for (int f = PL_FWD_RHO; f <= PL_FWD_TEM; ++f)
         if (!h->fld[f]) return fail(PL_ERR_STATE, "forward solution not set (pl_freeze_forward / pl_load)");
     int r;
@@ -1496,17 +1600,21 @@ static int filter_common(pl_lattice h, int op, double R, double beta, const doub
 }
 
 int pl_heaviside_var(pl_lattice h, double R, double beta, const double *s, const int *mask, double *out) {
+    PL_RANGE("pl_heaviside_var");
     return filter_common(h, 0, R, beta, s, nullptr, mask, out);
 }
 int pl_heaviside_sens(pl_lattice h, double R, double beta, const double *s, const double *dfdrho, const int *mask,
                       double *out) {
+    PL_RANGE("pl_heaviside_sens");
     return filter_common(h, 1, R, beta, s, dfdrho, mask, out);
 }
 int pl_density_filter(pl_lattice h, double R, const double *v, const int *mask, double *out) {
+    PL_RANGE("pl_density_filter");
     return filter_common(h, 2, R, 0.0, v, nullptr, mask, out);
 }
 
 int pl_normalize(pl_lattice h, double *v, int n) {
+    PL_RANGE("pl_normalize");
     if (!h || !v || n < 1 || n > h->n * h->q) return fail(PL_ERR_ARG, "bad arguments");
     double *buf;
     int r = scratch(h, 6, &buf);

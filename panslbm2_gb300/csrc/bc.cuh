@@ -116,7 +116,8 @@ __device__ __forceinline__ void apply_op(const Op &op, T *f, T *g, int node, con
         const T S = sT + T(2) * sO;
         T rho0;
         if (op.kind == BC_NS_U) {
-            u[0] = T(op.v0); u[1] = T(op.v1); if (ND == 3) u[2] = T(op.v2);
+            // uscale: time-varying inflow u(t) = uscale * u (1 = the reference routine)
+            u[0] = T(a.uscale * op.v0); u[1] = T(a.uscale * op.v1); if (ND == 3) u[2] = T(a.uscale * op.v2);
             rho0 = S / (d < 0 ? T(1) - u[A] : T(1) + u[A]);
         } else {
             rho0 = T(op.v0);
@@ -199,7 +200,7 @@ __device__ __forceinline__ void apply_op(const Op &op, T *f, T *g, int node, con
             for (int c = 1; c < Q; ++c) if (cmp<L>(c, A) == d) p[c] = src[opp_d<L>(c)] - rho0;
             break;
         }
-        const T u[3] = {T(op.v0), T(op.v1), ND == 3 ? T(op.v2) : T(0)};
+        const T u[3] = {T(a.uscale * op.v0), T(a.uscale * op.v1), ND == 3 ? T(a.uscale * op.v2) : T(0)};
         if (ND == 2) {
             const T un = u[0], ut = A == 0 ? u[1] : u[0];   // y edges use ux twice (reference)
             const int b = 1 - A;

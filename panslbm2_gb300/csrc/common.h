@@ -109,6 +109,11 @@ struct KArgs {
     const void *alpha, *kappa, *beta, *dirx, *diry, *dirz;   // design fields, compute type
     const void *fwd[5];         // adjoint kinds: forward rho, ux, uy, uz, tem (compute type)
     const void *elrho, *gamma;  // elastic kinds: density and stress scale (compute type)
+    // forced-convection heat-sink extension (compute type, null = off): AD_FORCE adds the
+    // volumetric heat source hsrc as w_c * hsrc to g; AAD_FORCE adds the volumetric objective
+    // weight objw (dJ/dT) to every adjoint g population
+    const void *hsrc, *objw;
+    double uscale;              // factor on the prescribed velocity of NS SetU / ANS iSetU ops
     double *out[11];            // macro outputs (forward: rho,ux,uy,uz,tem,qx,qy,qz;
                                 //  adjoint: ip,iux,iuy,iuz,imx,imy,imz,item,iqx,iqy,iqz;
                                 //  EL: ux,uy in 1,2 and sxx,sxy,syx,syy in 4..7;

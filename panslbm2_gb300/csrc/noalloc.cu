@@ -13,8 +13,12 @@
 //  * scratch: g_scratch holds kMaxPartials FP64 partial pairs (one per reduction block; the
 //    reduction never uses more blocks than that) and the three results; g_nonfinite is the
 //    non-finite flag of the first pass. Every partial and result is written before it is read;
-//    the flag is cleared by each call before its kernels run. Nothing has to be zeroed by the
-//    caller.
+//    the flag is cleared by each call before its kernels run and read back with the results:
+//    a non-finite input value makes the call return PL_ERR_NONFINITE (the status the solve
+//    loop reports as divergence), with *out still set. Nothing has to be zeroed by the caller.
+//  * pointers: a[m] and b[m] must be device memory of the current device, or managed memory;
+//    host memory and device memory of another GPU are rejected with PL_ERR_ARG before any
+//    kernel runs.
 //  * setup: the first call on a device, with that device current, looks the two symbols up
 //    (cudaGetSymbolAddress) and keeps their addresses; later calls on that device reuse them.
 //    Make the first call on each device before beginning any stream capture on it.
@@ -55,13 +59,16 @@ int cuda_err(const char *what, cudaError_t e) {
     return pl::record_error(PL_ERR_CUDA, buf);
 }
 
-bool device_readable(const void *p) {
+// memory the current device `dev` can read without peer access: its own device memory, or
+// managed memory
+bool device_readable(const void *p, int dev) {
     cudaPointerAttributes at;
     if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
         cudaGetLastError();
         return false;
     }
-    return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+    if (at.type == cudaMemoryTypeManaged) return true;
+    return at.type == cudaMemoryTypeDevice && at.device == dev;
 }
 
 }  // namespace
@@ -73,14 +80,13 @@ extern "C" int pl_residual_device_noalloc(long long n, int ncomp, const double *
     if (n < 1) return err(PL_ERR_ARG, "n must be at least 1");
     const int nblk = pl::resid_blocks(n);
     if (nblk > kMaxPartials) return err(PL_ERR_ARG, "reduction needs more partials than the static scratch holds");
-    for (int m = 0; m < ncomp; ++m)
-        if (!device_readable(a[m]) || !device_readable(b[m]))
-            return err(PL_ERR_ARG, "a[m] and b[m] must be device (or managed) pointers");
-
     int dev = -1;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return cuda_err("cudaGetDevice", e);
     if (dev < 0 || dev >= kMaxDevices) return err(PL_ERR_ARG, "device ordinal beyond the supported range");
+    for (int m = 0; m < ncomp; ++m)
+        if (!device_readable(a[m], dev) || !device_readable(b[m], dev))
+            return err(PL_ERR_ARG, "a[m] and b[m] must be device pointers of the current device (or managed)");
     double *scratch;
     int *flag;
     {
@@ -108,9 +114,13 @@ extern "C" int pl_residual_device_noalloc(long long n, int ncomp, const double *
     pl::launch_residual(ra, scratch, nblk, flag, scratch + kResultOffset, st);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_err("residual launch", e);
     double o[3];
+    int nonfinite = 0;
     if ((e = cudaMemcpyAsync(o, scratch + kResultOffset, sizeof o, cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+        return cuda_err("cudaMemcpyAsync", e);
+    if ((e = cudaMemcpyAsync(&nonfinite, flag, sizeof nonfinite, cudaMemcpyDeviceToHost, st)) != cudaSuccess)
         return cuda_err("cudaMemcpyAsync", e);
     if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_err("cudaStreamSynchronize", e);
     *out = o[2];
+    if (nonfinite) return err(PL_ERR_NONFINITE, "non-finite value in the residual inputs");
     return PL_OK;
 }

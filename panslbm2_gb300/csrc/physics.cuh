@@ -168,6 +168,18 @@ template <class L, class T> __device__ __forceinline__ void aad_heatex(T *g, T i
 #pragma unroll
     for (int c = 0; c < L::Q; ++c) g[c] -= coef;
 }
+// Volumetric heat source of the forced-convection heat sink (no reference routine): g_c += w_c Q,
+// the form of the heat-exchange term with a fixed source
+template <class L, class T> __device__ __forceinline__ void ad_source(T *g, T qsrc) {
+#pragma unroll
+    for (int c = 0; c < L::Q; ++c) g[c] += wt<L, T>(c) * qsrc;
+}
+// Its adjoint objective source: J = sum_x w(x) T(x) gives dJ/dg_c = w for every c, added in the
+// convention of the heat-exchange adjoint above (whose "1" is its objective's derivative)
+template <class L, class T> __device__ __forceinline__ void aad_objsrc(T *g, T w) {
+#pragma unroll
+    for (int c = 0; c < L::Q; ++c) g[c] += w;
+}
 // AAD::ExternalForceNaturalConvection (adjointadvection.h:114-132)
 template <class L, class T> __device__ __forceinline__ void aad_nc(T *g, const T *im, const T *gv) {
     const T coef = T(3) * vdot<L, T>(im, gv);
@@ -412,6 +424,7 @@ __device__ __forceinline__ void collide_node(T *f, T *g, int idx, const KArgs &a
             ns_brinkman<L, T>(f, rho, u, ldT<T>(a.alpha, idx));
             ns_macro<L, T>(f, rho, u);
             if (K == K_AD_HEATEX) ad_heatex<L, T>(g, tem, ldT<T>(a.beta, idx));
+            if (K == K_AD_FORCE && a.hsrc) ad_source<L, T>(g, ldT<T>(a.hsrc, idx));
             if (kind_has_g(K)) ad_macro<L, T>(g, u, omg, tem, q);
         } else if (K == K_AD_NATURAL) {
             ad_nc_force<L, T>(f, tem, gv[0], gv[1], gv[2], T(a.ph.tem0));
@@ -471,6 +484,9 @@ __device__ __forceinline__ void collide_node(T *f, T *g, int idx, const KArgs &a
                 aad_macro<L, T>(g, item, iq);
             } else if (K == K_AAD_HEATEX) {
                 aad_heatex<L, T>(g, item, ldT<T>(a.beta, idx));
+                aad_macro<L, T>(g, item, iq);
+            } else if (K == K_AAD_FORCE && a.objw) {
+                aad_objsrc<L, T>(g, ldT<T>(a.objw, idx));
                 aad_macro<L, T>(g, item, iq);
             }
         }

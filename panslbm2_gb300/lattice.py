@@ -107,8 +107,12 @@ class LatticePair:
         return out
 
     def set_field(self, f, v):
+        """upload field f; v = None switches the source fields (HEAT_SOURCE, OBJ_WEIGHT) off"""
         v = _f64(v, self.n)
         check(self.lib.pl_set_field(self.h, f, _dp(v)))
+
+    def set_inflow_scale(self, s):
+        check(self.lib.pl_set_inflow_scale(self.h, C.c_double(s)))
 
     def get_field(self, f):
         out = np.empty(self.n)

@@ -7,7 +7,9 @@ F_KINDS = (A.BC_NS_U, A.BC_NS_RHO, A.BC_ANS_U, A.BC_ANS_RHO, A.BC_AAD_RHO, A.BC_
            A.BC_EL_STRESS, A.BC_AEL_STRESS)
 
 
-def replay(o, L, f, g, ops, n, ux=None, uy=None, uz=None, rho=None, tem=None, kappa=None):
+def replay(o, L, f, g, ops, n, ux=None, uy=None, uz=None, rho=None, tem=None, kappa=None, uscale=1.0):
+    """Apply the op list in call order; `uscale` multiplies the prescribed velocity of NS SetU /
+    ANS iSetU ops (time-varying inflow)."""
     for op in ops:
         k = op["kind"]
         lat = op.get("lat", 0)
@@ -36,4 +38,4 @@ def replay(o, L, f, g, ops, n, ux=None, uy=None, uz=None, rho=None, tem=None, ka
         brho = vals["v2"] if k == A.BC_AEL_STRESS else rho
         o.apply_bc(L, tgt, k, op["axis"], op["pos"], op["dir"], ty, g=(g if k == A.BC_AAD_RHO else None),
                    ux=ux, uy=uy, uz=uz, rho=brho, tem=tem, diffusivity=kappa, kappa=op.get("kappa", 0.0),
-                   eps=op.get("eps", 0.0), **vals)
+                   eps=op.get("eps", 0.0), uscale=uscale, **vals)
