@@ -332,6 +332,46 @@ int pl_mma_set_state(pl_mma h, int k, double previous, const double *xkm2, const
  * error handling; nothing on the device faults. */
 int pl_debug_fail_alloc(long long after);
 
+/* Learned warm start (no counterpart in the reference): a 3D convolutional U-Net over an
+ * nx x ny x nz volume in the lattice's node order, trained and evaluated on the GPU's tensor
+ * cores (tcgen05 implicit-GEMM convolutions, BF16 weights and activations, FP32 accumulation,
+ * Adam on FP32 master weights). `levels` resolution levels with base_channels * 2^l channels
+ * (each volume extent divisible by 2^(levels-1)); 16 input channels (channel 0 = the design,
+ * channels 1.. = static features) and 16 output channels (the first `targets` are trained).
+ * Parameters are flattened per layer as weights [cout][taps][cin] then biases [cout], layers
+ * in the order encoder (level 0..L-1: conv1, conv2), decoder (level L-2..0: conv1, conv2),
+ * head (1x1x1). */
+typedef struct pl_unet_s *pl_unet;
+int pl_unet_create(int nx, int ny, int nz, int levels, int base_channels, int in_channels, int out_channels,
+                   int max_batch, pl_unet *out);
+int pl_unet_destroy(pl_unet u);
+long long pl_unet_param_count(pl_unet u);
+int pl_unet_init_params(pl_unet u, unsigned long long seed);
+int pl_unet_get_params(pl_unet u, float *host);
+int pl_unet_set_params(pl_unet u, const float *host);
+/* one forward pass on host inputs x [batch][voxel][16] (FP32, rounded to BF16) -> y [batch][voxel][16] */
+int pl_unet_forward(pl_unet u, int batch, const float *x_host, float *y_host);
+/* the backward pass of the last forward for dL/dy = dy [batch][voxel][16]; the parameter
+ * gradients are read with pl_unet_gradients (same layout as the parameters) */
+int pl_unet_backward(pl_unet u, int batch, const float *dy_host);
+int pl_unet_gradients(pl_unet u, float *host);
+/* training set on the device: `nsamples` (design, targets) pairs; static features [voxel][nfeat]
+ * (nfeat <= 15) shared by all samples; pl_unet_add_sample stores one design (nvox doubles) and
+ * its targets [targets][nvox] */
+int pl_unet_dataset_reserve(pl_unet u, int nsamples, int targets);
+int pl_unet_set_static(pl_unet u, const float *feat, int nfeat);
+int pl_unet_add_sample(pl_unet u, int slot, const double *design, const double *targets);
+/* train on samples 0..nsamples-1 (targets normalised per channel over them) for `epochs`
+ * shuffled passes of mini-batches; loss_per_epoch (may be NULL) receives the mean squared error
+ * of the normalised targets per epoch */
+int pl_unet_train(pl_unet u, int nsamples, int epochs, int batch, double lr, unsigned long long seed,
+                  double *loss_per_epoch);
+/* the target normalisation (mean, std per target channel), e.g. to restore a trained model */
+int pl_unet_set_norm(pl_unet u, const float *mean, const float *stdv);
+int pl_unet_get_norm(pl_unet u, float *mean, float *stdv);
+/* prediction for one design: out [targets][nvox] (de-normalised, FP64) */
+int pl_unet_predict(pl_unet u, const double *design, double *out);
+
 /* last step kernel time (ms) measured with CUDA events on the lattice stream, and number
  * of kernels launched since creation */
 int pl_stats(pl_lattice h, double *last_step_ms, long long *launches);

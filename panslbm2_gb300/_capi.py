@@ -65,6 +65,10 @@ EXPORTS = [
     "pl_sensitivity_device", "pl_accumulate", "pl_heaviside_var",
     "pl_heaviside_sens", "pl_density_filter", "pl_normalize", "pl_stats", "pl_mma_create", "pl_mma_set_param",
     "pl_mma_update", "pl_mma_destroy", "pl_mma_get_state", "pl_mma_set_state", "pl_debug_fail_alloc",
+    "pl_unet_create", "pl_unet_destroy", "pl_unet_param_count", "pl_unet_init_params", "pl_unet_get_params",
+    "pl_unet_set_params", "pl_unet_forward", "pl_unet_backward", "pl_unet_gradients", "pl_unet_dataset_reserve",
+    "pl_unet_set_static", "pl_unet_add_sample", "pl_unet_train", "pl_unet_set_norm", "pl_unet_get_norm",
+    "pl_unet_predict",
 ]
 
 _lib = None
