@@ -1,27 +1,36 @@
-"""Throughput of the fused NS+AD lattice-Boltzmann step on GB300 (one JSON line on rank 0).
+"""Throughput of the fused NS+AD lattice-Boltzmann step on GB300 (one JSON line on rank 0), and
+the benchmark configurations around it.
 
-Workload (default): the 3D steady heat sink, coupled D3Q15 NS + D3Q15 advection-diffusion,
-160x160x80 lattice (2,048,000 nodes), FP32 populations and compute, Brinkman + natural
-convection collide (AD::MacroBrinkmanCollideNaturalConvection) with the production driver's
-boundary program (walls, Dirichlet T, heat-flux Q, corner/edge smoothing) every step, design
-from a seeded Gaussian random field (correlation length 8 cells). A bench "step" is one fused
-time step over the whole lattice: pull-stream + boundary program + collide. The population
-buffers (2 x 245 MB) exceed the 129 MB L2, so no flush is needed between steps.
+Workload (default): the 3D steady forced-convection heat sink, coupled D3Q15 NS + D3Q15
+advection-diffusion, 160x160x80 lattice (2,048,000 nodes), FP32 populations and compute:
+Brinkman + forced-convection collide (AD::MacroBrinkmanCollideForceConvection) with the
+volumetric heat source of a 40x4x40 base plate, the boundary program of parabolic inflow,
+pressure outlet with zero temperature gradient, walls and corner smoothing every step; design
+from a seeded Gaussian random field (correlation length 8 cells). A bench "step" is one fused time
+step over the whole lattice: pull-stream + boundary program + collide. The population buffers
+(2 x 245 MB) exceed the 129 MB L2, so no flush is needed between steps.
 
-  value        MLUPS of the device-resident fused step (sum over ranks; replicas)
-  e2e          MLUPS through the C ABI with host buffers: per e2e step, upload alpha/kappa
-               from pinned host memory, run one residual-check interval of 100 time steps
-               (pl_solve), download T and u
-  roofline     HBM: 248 algorithmic bytes per node per step (read + write 2 x 15 FP32
-               populations, read alpha and kappa) / measured step time, vs MEASURED_PEAKS
-  cpu_baseline the C restatement of the reference's scalar OpenMP path (oracle/), FP64, on
-               the host cores, on a bounded number of steps of the same workload
-  design_iter_3d the same design iteration, plain method, on the 160x160x80 FP32 lattice
+  value          MLUPS of the device-resident fused step (sum over ranks; replicas)
+  e2e            MLUPS through the C ABI with host buffers: per e2e step, upload alpha / kappa
+                 from pinned host memory, run one residual-check interval of 100 time steps
+                 (pl_solve), download T and u
+  roofline       HBM: algorithmic bytes per node per step (read + write 2 x 15 FP32 populations,
+                 read alpha, kappa and the heat source) / measured step time, vs MEASURED_PEAKS
+  cpu_baseline   the C restatement of the reference's scalar OpenMP path (oracle/), FP64, on the
+                 host cores: one warm-up step, then the median of 5 timed spans
+  config1_cavity the 100x100 lid-driven cavity, 20,000 steps, FP64, GPU and the CPU port timed,
+                 and their largest difference
+  design_iter    one design iteration of the 200x100 FP64 forced-convection heat sink (filter,
+                 forward and adjoint to residual 1e-6, sensitivity, filtered sensitivity) on the
+                 GPU, and the CPU port's forward + adjoint on the same step counts (timed within a
+                 budget, extrapolated beyond it and labelled so)
+  design_iter_3d_surrogate  the 160x160x80 FP32 design iteration, plain (from rest) and with the
+                 learned warm start (trained weights in panslbm2_gb300/weights/), to the same
+                 residual tolerance
+  precision_errors  objective and sensitivity errors of FP32, FP16 and BF16 storage against FP64 on
+                 the 1600x800 forced-convection heat sink
   transient_iter seconds of one transient heat-sink evaluation (4000 time steps forward and
-               adjoint, checkpoints every 100 steps) on the 192x192x96 FP32 lattice
-  design_iter  seconds of one heat-sink design iteration (filter, forward and adjoint to residual
-               1e-6, sensitivity, filtered sensitivity) on the 200x100 FP64 lattice, with the
-               oracle port's time for the same step counts
+                 adjoint, checkpoints every 100 steps) on the 192x192x96 FP32 lattice
 
 --impl reference times that CPU path alone: the reference's own implementation of the path is
 header-only C++ whose sources are not present on the GPU host, so the restatement stands in.
@@ -40,32 +49,63 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 WORKLOADS = {
-    "heatsink3d-160x160x80-fp32": dict(nd=3, lx=160, ly=160, lz=80, storage="fp32"),
-    "heatsink3d-192x192x96-fp32": dict(nd=3, lx=192, ly=192, lz=96, storage="fp32"),
-    "heatsink2d-1600x800-fp32": dict(nd=2, lx=1600, ly=800, lz=1, storage="fp32"),
-    "heatsink2d-1600x800-fp64": dict(nd=2, lx=1600, ly=800, lz=1, storage="fp64"),
-    "heatsink2d-1600x800-fp16": dict(nd=2, lx=1600, ly=800, lz=1, storage="fp16"),
-    "heatsink2d-1600x800-bf16": dict(nd=2, lx=1600, ly=800, lz=1, storage="bf16"),
-    "heatsink3d-160x160x80-fp16": dict(nd=3, lx=160, ly=160, lz=80, storage="fp16"),
-    "heatsink3d-160x160x80-bf16": dict(nd=3, lx=160, ly=160, lz=80, storage="bf16"),
+    "forced3d-160x160x80-fp32": dict(phys="forced", nd=3, lx=160, ly=160, lz=80, storage="fp32"),
+    "forced3d-192x192x96-fp32": dict(phys="forced", nd=3, lx=192, ly=192, lz=96, storage="fp32"),
+    "forced3d-160x160x80-fp16": dict(phys="forced", nd=3, lx=160, ly=160, lz=80, storage="fp16"),
+    "forced3d-160x160x80-bf16": dict(phys="forced", nd=3, lx=160, ly=160, lz=80, storage="bf16"),
+    "forced2d-1600x800-fp64": dict(phys="forced", nd=2, lx=1600, ly=800, lz=1, storage="fp64"),
+    "forced2d-1600x800-fp32": dict(phys="forced", nd=2, lx=1600, ly=800, lz=1, storage="fp32"),
+    "forced2d-1600x800-fp16": dict(phys="forced", nd=2, lx=1600, ly=800, lz=1, storage="fp16"),
+    "forced2d-1600x800-bf16": dict(phys="forced", nd=2, lx=1600, ly=800, lz=1, storage="bf16"),
+    "heatsink3d-160x160x80-fp32": dict(phys="natural", nd=3, lx=160, ly=160, lz=80, storage="fp32"),
+    "heatsink3d-192x192x96-fp32": dict(phys="natural", nd=3, lx=192, ly=192, lz=96, storage="fp32"),
+    "heatsink3d-160x160x80-fp16": dict(phys="natural", nd=3, lx=160, ly=160, lz=80, storage="fp16"),
+    "heatsink3d-160x160x80-bf16": dict(phys="natural", nd=3, lx=160, ly=160, lz=80, storage="bf16"),
+    "heatsink2d-1600x800-fp32": dict(phys="natural", nd=2, lx=1600, ly=800, lz=1, storage="fp32"),
+    "heatsink2d-1600x800-fp64": dict(phys="natural", nd=2, lx=1600, ly=800, lz=1, storage="fp64"),
 }
-DEFAULT = "heatsink3d-160x160x80-fp32"
+DEFAULT = "forced3d-160x160x80-fp32"
 METRIC = "fused NS+AD MLUPS"
 
 
-def bytes_per_node(q, storage):
-    s = {"fp64": 8, "fp32": 4, "fp16": 2, "bf16": 2}[storage]
-    c = 8 if storage == "fp64" else 4
-    return 2 * 2 * q * s + 2 * c
+class Setup:
+    """the step workload: kind, physics constants, design fields, boundary program"""
 
+    def __init__(self, wl, seed=0):
+        from panslbm2_gb300 import _capi as A
+        from panslbm2_gb300 import heatsink as HS
+        from panslbm2_gb300 import forced as FC
+        nd, lx, ly, lz = wl["nd"], wl["lx"], wl["ly"], wl["lz"]
+        self.nd, self.lx, self.ly, self.lz = nd, lx, ly, lz
+        self.q = 9 if nd == 2 else 15
+        self.n = lx * ly * lz
+        self.storage = wl["storage"]
+        ss = HS.grf_design(nd, lx, ly, lz, seed=seed, sigma=8.0)
+        if wl["phys"] == "forced":
+            p = FC.ForcedParams(nd, lx, ly, lz)
+            ss = p.project(ss)
+            alpha, kappa, _, _ = p.design_fields(ss)
+            self.fields = {A.ALPHA: alpha, A.KAPPA: kappa, A.HEAT_SOURCE: p.heat_source(ss)[0]}
+            self.ops = p.program_ops("forward")
+            self.kind = A.AD_FORCE
+            self.phys = dict(nu=p.nu, diff=0.0, gx=0.0, gy=0.0, gz=0.0, tem0=0.0)
+            self.oracle_fields = dict(alpha=alpha, diffusivity=kappa, hsrc=self.fields[A.HEAT_SOURCE])
+            self.nfield = 3
+        else:
+            p = HS.Params(nd, lx, ly, lz)
+            alpha, kappa, _, _ = p.design_fields(ss)
+            self.fields = {A.ALPHA: alpha, A.KAPPA: kappa}
+            self.ops = HS.program_ops("forward", p)
+            self.kind = A.AD_NATURAL
+            self.phys = dict(nu=p.nu, diff=0.0, gx=p.gx, gy=p.gy, gz=p.gz, tem0=p.tem0)
+            self.oracle_fields = dict(alpha=alpha, diffusivity=kappa)
+            self.nfield = 2
+        self.p = p
 
-def setup(wl, seed=0):
-    from panslbm2_gb300 import heatsink as HS
-    p = HS.Params(wl["nd"], wl["lx"], wl["ly"], wl["lz"])
-    ss = HS.grf_design(wl["nd"], wl["lx"], wl["ly"], wl["lz"], seed=seed, sigma=8.0)
-    alpha, kappa, dads, dkds = p.design_fields(ss)
-    ops = HS.program_ops("forward", p)
-    return p, alpha, kappa, ops
+    def bytes_per_node(self):
+        s = {"fp64": 8, "fp32": 4, "fp16": 2, "bf16": 2}[self.storage]
+        c = 8 if self.storage == "fp64" else 4
+        return 2 * 2 * self.q * s + self.nfield * c
 
 
 class Clocks:
@@ -145,80 +185,208 @@ def traffic_per_node(workload):
     return None
 
 
-def cpu_port(p, alpha, kappa, ops, q, budget_s=12.0, max_steps=30):
-    """Time the oracle restatement of the reference's scalar OpenMP path (FP64) on the host."""
+def host_info():
+    return {"nproc": os.cpu_count(), "omp_proc_bind": os.environ.get("OMP_PROC_BIND", "close"),
+            "machine": os.uname().machine}
+
+
+def cpu_port(S, spans=5, steps_per_span=None, budget_s=12.0):
+    """The oracle restatement of the reference's scalar OpenMP path (FP64) on the host: one
+    warm-up step, then the median of `spans` timed spans of the same workload."""
+    os.environ.setdefault("OMP_PROC_BIND", "close")
     from oracle.olib import Oracle
     from panslbm2_gb300 import _capi as A
-    sys.path.insert(0, os.path.join(ROOT, "tests"))
-    from _replay import replay
+    from tests._replay import replay
     o = Oracle("oracle")
     cores = os.cpu_count() or 1
     o.set_threads(cores)
-    L = o.lat(q, p.lx, p.ly, p.lz)
-    n = p.lx * p.ly * p.lz
+    q, n = S.q, S.n
+    L = o.lat(q, S.lx, S.ly, S.lz)
     f, g = np.zeros((q, n)), np.zeros((q, n))
     one, zero = np.ones(n), np.zeros(n)
     o.init(L, 0, f, o.fields(rho=one, ux=zero, uy=zero, uz=zero))
     o.init(L, 1, g, o.fields(tem=zero, ux=zero, uy=zero, uz=zero))
     mac = {k: np.zeros(n) for k in ("rho", "ux", "uy", "uz", "tem", "qx", "qy", "qz")}
-    ph = dict(nu=p.nu, diff=0.0, gx=p.gx, gy=p.gy, gz=p.gz, tem0=p.tem0)
-    F = o.fields(alpha=alpha, diffusivity=kappa, **mac)
+    F = o.fields(**S.oracle_fields, **mac)
+    kappa = S.oracle_fields["diffusivity"]
 
     def one_step():
-        o.collide(L, A.AD_NATURAL, f, g, F, **ph, save=True)
+        o.collide(L, S.kind, f, g, F, **S.phys, save=True)
         o.stream(L, f)
         o.stream(L, g)
-        replay(o, L, f, g, ops, n, ux=mac["ux"], uy=mac["uy"], uz=mac["uz"], kappa=kappa)
+        replay(o, L, f, g, S.ops, n, ux=mac["ux"], uy=mac["uy"], uz=mac["uz"], kappa=kappa)
 
+    t0 = time.perf_counter()
     one_step()   # warm-up
-    t0, steps = time.perf_counter(), 0
-    while steps < max_steps and (time.perf_counter() - t0) < budget_s:
-        one_step()
-        steps += 1
-    dt = time.perf_counter() - t0
-    return {"value": n * steps / dt / 1e6, "unit": "MLUPS", "cores": cores, "kind": "port",
-            "sample": "%d full time steps (collide + 2 streams + boundary program) of the %dx%dx%d lattice, FP64"
-                      % (steps, p.lx, p.ly, p.lz)}
+    t1 = time.perf_counter() - t0
+    if steps_per_span is None:
+        steps_per_span = max(1, min(30, int(budget_s / spans / max(t1, 1e-6))))
+    rates = []
+    for _ in range(spans):
+        t0 = time.perf_counter()
+        for _ in range(steps_per_span):
+            one_step()
+        rates.append(n * steps_per_span / (time.perf_counter() - t0) / 1e6)
+    return {"value": float(np.median(rates)), "unit": "MLUPS", "cores": cores, "kind": "port",
+            "spans_mlups": [round(r, 2) for r in rates], "method": "1 warm-up step, median of %d spans" % spans,
+            "host": host_info(),
+            "sample": "%d spans of %d full time steps (collide + 2 streams + boundary program) of the %dx%dx%d "
+                      "lattice, FP64" % (spans, steps_per_span, S.lx, S.ly, S.lz)}
 
 
-DESIGN_LATTICE = dict(nd=2, lx=200, ly=100, lz=1, storage="fp64")
+def cavity_leg():
+    """config 1: the 100x100 lid-driven cavity, 20,000 steps, FP64: GPU and CPU port"""
+    from oracle.olib import Oracle
+    from panslbm2_gb300 import forced as FC
+    from tests import _forced_oracle as FO
+    FC.run_cavity(100, 100, 200)   # warm-up
+    rho, ux, uy, sec = FC.run_cavity(100, 100, 20000, storage="fp64")
+    o = Oracle("oracle")
+    o.set_threads(os.cpu_count() or 1)
+    t0 = time.perf_counter()
+    mac = FO.cavity(o, 100, 100, 20000)
+    cpu = time.perf_counter() - t0
+    diff = max(float(np.max(np.abs(a - mac[k])) / np.max(np.abs(mac[k]))) for a, k in ((rho, "rho"), (ux, "ux"),
+                                                                                        (uy, "uy")))
+    return {"lattice": "cavity2d-100x100-fp64", "steps": 20000, "gpu_seconds": round(sec, 4),
+            "gpu_mlups": round(1e4 * 2e4 / sec / 1e6, 1), "cpu_seconds": round(cpu, 3),
+            "cpu_kind": "port, FP64, %d host threads" % (os.cpu_count() or 1),
+            "max_rel_diff_gpu_vs_cpu": diff}
 
 
-def design_gpu(tol=1e-6, max_steps=100000):
-    """One heat-sink design iteration (filter, forward and adjoint to `tol`, sensitivity, filtered
-    and normalised sensitivity) through the library, on the 200x100 FP64 lattice."""
-    from panslbm2_gb300 import heatsink as HS
-    from panslbm2_gb300.design import HeatSinkDesign
-    d = DESIGN_LATTICE
-    p = HS.Params(d["nd"], d["lx"], d["ly"], d["lz"])
-    s = HS.grf_design(d["nd"], d["lx"], d["ly"], d["lz"], seed=0, sigma=8.0)
-    hs = HeatSinkDesign(p, d["storage"])
-    hs.iterate(s, tol=tol, max_steps=2000)          # warm-up: builds the filter taps and programs
-    r = hs.iterate(s, tol=tol, max_steps=max_steps)
-    hs.close()
-    return p, s, r
-
-
-def design_gpu_3d(tol=1e-6, max_steps=100000):
-    """The plain design iteration on the 160x160x80 FP32 lattice (the learned warm start's
-    comparison point): filter, forward and adjoint from rest to `tol`, sensitivity."""
-    from panslbm2_gb300 import heatsink as HS
-    from panslbm2_gb300.design import HeatSinkDesign
-    p = HS.Params(3, 160, 160, 80)
-    s = HS.grf_design(3, 160, 160, 80, seed=0, sigma=8.0)
-    hs = HeatSinkDesign(p, "fp32")
-    hs.iterate(s, tol=tol, max_steps=200)          # warm-up: filter taps, programs
-    r = hs.iterate(s, tol=tol, max_steps=max_steps)
-    hs.close()
+def design_leg(cpu=True, cpu_budget_s=45.0):
+    """config 2: one forced-convection design iteration on 200x100 FP64 (filter, forward and
+    adjoint to 1e-6, sensitivity, filtered sensitivity); the CPU port's forward + adjoint on the
+    same step counts"""
     from panslbm2_gb300 import _capi as A
-    return {"lattice": "heatsink3d-160x160x80-fp32", "tol": tol, "max_steps": max_steps,
-            "seconds": round(r["seconds"]["total"], 3),
-            "phases_s": {k: round(v, 3) for k, v in r["seconds"].items()},
-            "forward_steps": r["forward"][1], "adjoint_steps": r["adjoint"][1],
-            "converged": [r["forward"][0] == A.PL_CONVERGED, r["adjoint"][0] == A.PL_CONVERGED],
-            "objective": r["objective"],
-            "what": "plain method from rest (no warm start): filter, forward and adjoint to the residual tolerance, "
-                    "heat-source sensitivity, filtered and normalised sensitivity"}
+    from panslbm2_gb300 import forced as FC
+    p = FC.ForcedParams(2, 200, 100)
+    s = p.design(seed=0)
+    hs = FC.ForcedHeatSink(p, "fp64")
+    hs.iterate(s, max_steps=1000)            # warm-up: filter taps, programs
+    r = hs.iterate(s, tol=1e-6, max_steps=100000)
+    hs.close()
+    out = {"lattice": "forced2d-200x100-fp64", "tol": 1e-6, "max_steps": 100000,
+           "seconds": round(r["seconds"]["total"], 4), "phases_s": {k: round(v, 4) for k, v in r["seconds"].items()},
+           "forward_steps": r["forward"][1], "adjoint_steps": r["adjoint"][1],
+           "converged": [r["forward"][0] == A.PL_CONVERGED, r["adjoint"][0] == A.PL_CONVERGED],
+           "objective": r["objective"],
+           "what": "filter, forward and adjoint to residual 1e-6 (checked every 100 steps), sensitivity, filtered "
+                   "sensitivity; from rest; no MMA update"}
+    if cpu:
+        out.update(design_cpu(p, r["ss"], r["forward"][1], r["adjoint"][1], cpu_budget_s))
+    return out
+
+
+def design_cpu(p, ss, nf, na, budget_s):
+    """the oracle port's forward and adjoint steps of the design iteration (FP64, all host
+    threads), timed up to `budget_s`; beyond it the measured rate is extrapolated"""
+    from oracle.olib import Oracle
+    from panslbm2_gb300 import _capi as A
+    from tests._replay import replay
+    o = Oracle("oracle")
+    o.set_threads(os.cpu_count() or 1)
+    q, n = 9, p.n
+    L = o.lat(q, p.lx, p.ly)
+    alpha, kappa, _, _ = p.design_fields(ss)
+    Q = p.heat_source(ss)[0]
+    w = p.objective_weight(ss)
+    f, g = np.zeros((q, n)), np.zeros((q, n))
+    zero = np.zeros(n)
+    o.init(L, 0, f, o.fields(rho=np.ones(n), ux=zero, uy=zero, uz=zero))
+    o.init(L, 1, g, o.fields(tem=zero, ux=zero, uy=zero, uz=zero))
+    mac = {k: np.zeros(n) for k in ("rho", "ux", "uy", "uz", "tem", "qx", "qy", "qz")}
+    ops_f, ops_a = p.program_ops("forward"), p.program_ops("adjoint")
+    F = o.fields(alpha=alpha, diffusivity=kappa, hsrc=Q, **mac)
+    t0 = time.perf_counter()
+    done_f = 0
+    while done_f < nf and time.perf_counter() - t0 < budget_s / 2:
+        if done_f:
+            o.stream(L, f)
+            o.stream(L, g)
+            replay(o, L, f, g, ops_f, n, ux=mac["ux"], uy=mac["uy"], uz=mac["uz"], kappa=kappa)
+        o.collide(L, A.AD_FORCE, f, g, F, nu=p.nu, save=True)
+        done_f += 1
+    tf = time.perf_counter() - t0
+    adj = {k: np.zeros(n) for k in ("ip", "iux", "iuy", "iuz", "imx", "imy", "imz", "item", "iqx", "iqy", "iqz")}
+    Fa = o.fields(alpha=alpha, diffusivity=kappa, objw=w, **mac, **adj)
+    o.init(L, 2, f, o.fields(ux=mac["ux"], uy=mac["uy"], uz=mac["uz"], ip=zero, iux=zero, iuy=zero, iuz=zero))
+    o.init(L, 3, g, o.fields(ux=mac["ux"], uy=mac["uy"], uz=mac["uz"], item=zero, iqx=zero, iqy=zero, iqz=zero))
+    t1 = time.perf_counter()
+    done_a = 0
+    while done_a < na and time.perf_counter() - t1 < budget_s / 2:
+        if done_a:
+            o.stream(L, f, True)
+            o.stream(L, g, True)
+            replay(o, L, f, g, ops_a, n, ux=mac["ux"], uy=mac["uy"], uz=mac["uz"], rho=mac["rho"], tem=mac["tem"],
+                   kappa=kappa)
+        o.collide(L, A.AAD_FORCE, f, g, Fa, nu=p.nu, save=True)
+        done_a += 1
+    ta = time.perf_counter() - t1
+    est = tf * nf / done_f + ta * na / done_a
+    full = done_f == nf and done_a == na
+    return {"cpu_seconds": round(est, 2), "cpu_timed_fully": full,
+            "cpu_sample": "oracle port, FP64, %d host threads: %d of %d forward and %d of %d adjoint steps timed%s" % (
+                os.cpu_count() or 1, done_f, nf, done_a, na, "" if full else ", the rest extrapolated at the measured "
+                                                                             "rate")}
+
+
+def surrogate_leg(tol=1e-5):
+    """config 4: plain vs learned warm start on 160x160x80 FP32, held-out design (seed 0)"""
+    from panslbm2_gb300 import _capi as A
+    from panslbm2_gb300 import forced as FC
+    from panslbm2_gb300.surrogate import SurrogateWarmStart, default_weights_path
+    path = default_weights_path()
+    if not os.path.exists(path):
+        return {"error": "no trained weights at %s" % os.path.relpath(path, ROOT)}
+    p = FC.ForcedParams(3, 160, 160, 80)
+    sw = SurrogateWarmStart(p, "fp32")
+    meta = sw.net.load(path)
+    s = p.design(seed=0)
+    sw.iterate(s, True, tol=1e-2, max_steps=300)    # warm-up: programs, taps, kernels
+    out = {"lattice": "forced3d-160x160x80-fp32", "tol": tol, "design_seed": 0,
+           "training": {k: meta.get(k) for k in ("nsamples", "epochs", "seeds")}}
+    for name, warm in (("plain", False), ("surrogate", True)):
+        r = sw.iterate(s, warm, tol=tol, max_steps=100000)
+        out[name] = {"seconds": round(r["seconds"]["total"], 3),
+                     "phases_s": {k: round(v, 3) for k, v in r["seconds"].items()},
+                     "forward_steps": r["forward"][1], "adjoint_steps": r["adjoint"][1],
+                     "converged": [r["forward"][0] == A.PL_CONVERGED, r["adjoint"][0] == A.PL_CONVERGED],
+                     "objective": r["objective"]}
+    sw.close()
+    a, b = out["plain"], out["surrogate"]
+    out["speedup"] = round(a["seconds"] / b["seconds"], 3)
+    out["step_ratio"] = round((a["forward_steps"] + a["adjoint_steps"]) / (b["forward_steps"] + b["adjoint_steps"]), 3)
+    out["objective_rel_diff"] = abs(a["objective"] - b["objective"]) / abs(a["objective"])
+    out["what"] = ("design iteration (filter, forward, adjoint, sensitivity) from rest vs from the U-Net's predicted "
+                   "fields, both to the same residual tolerance; FP32 residuals on this lattice level off near 4e-6, "
+                   "so the comparison is at 1e-5")
+    return out
+
+
+def precision_leg(nf=4000, na=4000):
+    """config 3: FP32 / FP16 / BF16 storage against FP64 on the 1600x800 forced heat sink"""
+    from panslbm2_gb300 import forced as FC
+    p = FC.ForcedParams(2, 1600, 800)
+    s = p.design(seed=0)
+    res = {}
+    for st in ("fp64", "fp32", "fp16", "bf16"):
+        hs = FC.ForcedHeatSink(p, st)
+        t0 = time.perf_counter()
+        res[st] = hs.iterate(s, fixed_steps=(nf, na))
+        res[st]["sec"] = time.perf_counter() - t0
+        hs.close()
+    b = res["fp64"]
+    out = {"lattice": "forced2d-1600x800", "forward_steps": nf, "adjoint_steps": na, "design_seed": 0,
+           "fp64_objective": b["objective"]}
+    for st in ("fp32", "fp16", "bf16"):
+        r = res[st]
+        out[st] = {"objective_rel_err": abs(r["objective"] - b["objective"]) / abs(b["objective"]),
+                   "sensitivity_rel_err_max": float(np.max(np.abs(r["dJdss"] - b["dJdss"])) / np.max(np.abs(b["dJdss"]))),
+                   "sensitivity_rel_err_l2": float(np.linalg.norm(r["dJdss"] - b["dJdss"]) / np.linalg.norm(b["dJdss"])),
+                   "seconds": round(r["sec"], 3)}
+    out["fp64_seconds"] = round(b["sec"], 3)
+    return out
 
 
 TRANSIENT_LATTICE = dict(nd=3, lx=192, ly=192, lz=96, storage="fp32", levels=4000, every=100)
@@ -250,62 +418,26 @@ def transient_gpu():
                     "forward states recomputed from device checkpoints; no filter or MMA"}
 
 
-def design_cpu_per_step(p, budget_s=8.0):
-    """Seconds per forward and per adjoint time step of the oracle port (FP64, all host cores) on
-    the design lattice, from a bounded sample of steps with the drivers' every-step saves."""
-    from oracle.olib import Oracle
-    from panslbm2_gb300 import _capi as A
-    from panslbm2_gb300 import heatsink as HS
-    sys.path.insert(0, os.path.join(ROOT, "tests"))
-    from _replay import replay
-    o = Oracle("oracle")
-    o.set_threads(os.cpu_count() or 1)
-    q = 9 if p.nd == 2 else 15
-    L = o.lat(q, p.lx, p.ly, p.lz)
-    n = p.lx * p.ly * p.lz
-    ss = HS.grf_design(p.nd, p.lx, p.ly, p.lz, seed=0, sigma=8.0)
-    alpha, kappa, _, _ = p.design_fields(ss)
-    ph = dict(nu=p.nu, diff=0.0, gx=p.gx, gy=p.gy, gz=p.gz, tem0=p.tem0)
-    out = {}
-    for phase, kind, inverse in (("forward", A.AD_NATURAL, False), ("adjoint", A.AAD_NATURAL, True)):
-        f, g = np.zeros((q, n)), np.zeros((q, n))
-        zero = np.zeros(n)
-        o.init(L, 0, f, o.fields(rho=np.ones(n), ux=zero, uy=zero, uz=zero))
-        o.init(L, 1, g, o.fields(tem=zero, ux=zero, uy=zero, uz=zero))
-        names = ("rho", "ux", "uy", "uz", "tem", "qx", "qy", "qz", "ip", "iux", "iuy", "iuz", "imx", "imy", "imz",
-                 "item", "iqx", "iqy", "iqz")
-        mac = {k: np.zeros(n) for k in names}
-        mac["rho"][:] = 1.0
-        snap = np.zeros(n * q)
-        ops = HS.program_ops(phase, p)
-        F = o.fields(gsnap=snap, alpha=alpha, diffusivity=kappa, **mac)
-        steps, t0 = 0, time.perf_counter()
-        while time.perf_counter() - t0 < budget_s and steps < 2000:
-            o.collide(L, kind, f, g, F, **ph, save=True)
-            o.stream(L, f, inverse)
-            o.stream(L, g, inverse)
-            replay(o, L, f, g, ops, n, ux=mac["ux"], uy=mac["uy"], uz=mac["uz"], rho=mac["rho"], tem=mac["tem"],
-                   kappa=kappa)
-            steps += 1
-        out[phase] = (time.perf_counter() - t0) / max(1, steps)
-        out[phase + "_sample"] = steps
-    return out
-
-
 def run_reference(args, wl):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    p, alpha, kappa, ops = setup(wl)
-    q = 9 if wl["nd"] == 2 else 15
-    cb = cpu_port(p, alpha, kappa, ops, q, budget_s=60.0, max_steps=max(1, min(args.steps, 40)))
+    S = Setup(wl)
+    cb = cpu_port(S, spans=5, budget_s=30.0)
     line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "MLUPS", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded GRF design)",
-            "config": {"workload": args.workload, "nodes": p.lx * p.ly * p.lz, "backend": "cpu"},
+            "config": {"workload": args.workload, "nodes": S.n, "backend": "cpu"},
             "cpu_baseline": cb, "e2e": {"value": cb["value"], "unit": "MLUPS", "h2d_bytes_per_step": 0,
                                         "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def leg(line, name, fn, *a, **k):
+    try:
+        line[name] = fn(*a, **k)
+    except Exception as e:   # reported, not fatal: the step throughput stands on its own
+        line[name] = {"error": ("%s: %s" % (type(e).__name__, e))[:300]}
 
 
 def main():
@@ -315,9 +447,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=50)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default=DEFAULT, choices=sorted(WORKLOADS))
-    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline legs")
     ap.add_argument("--e2e-steps", type=int, default=5)
-    ap.add_argument("--no-design", action="store_true", help="skip the design-iteration timing")
+    ap.add_argument("--no-design", action="store_true", help="skip the configuration legs (cavity, design, "
+                                                             "surrogate, precision)")
     ap.add_argument("--no-transient", action="store_true", help="skip the transient-evaluation timing")
     args = ap.parse_args()
     wl = WORKLOADS[args.workload]
@@ -337,22 +470,21 @@ def main():
     from panslbm2_gb300 import heatsink as HS
     from panslbm2_gb300.lattice import LatticePair, phys
 
-    p, alpha, kappa, ops = setup(wl, seed=rank)
-    q = 9 if wl["nd"] == 2 else 15
-    n = p.lx * p.ly * p.lz
+    S = Setup(wl, seed=rank)
+    q, n = S.q, S.n
     zero, one = np.zeros(n), np.ones(n)
-    lp = LatticePair(q, p.lx, p.ly, p.lz, wl["storage"])
+    lp = LatticePair(q, S.lx, S.ly, S.lz, S.storage)
     stream = torch.cuda.Stream()    # a created stream: capturable into the library's CUDA graphs
     torch.cuda.set_stream(stream)
     lp.set_stream(stream.cuda_stream)
-    lp.set_field(A.ALPHA, alpha)
-    lp.set_field(A.KAPPA, kappa)
+    for fid, v in S.fields.items():
+        lp.set_field(fid, v)
     lp.init(0, one, ux=zero, uy=zero, uz=zero)
     lp.init(1, zero, ux=zero, uy=zero, uz=zero)
-    prog = lp.program(HS.to_descs(ops))
-    ph = phys(nu=p.nu, diff=0.0, gx=p.gx, gy=p.gy, gz=p.gz, tem0=p.tem0)
-    lp.collide(A.AD_NATURAL, ph)
-    lp.steps(A.AD_NATURAL, ph, prog, max(3, args.warmup))
+    prog = lp.program(HS.to_descs(S.ops))
+    ph = phys(**S.phys)
+    lp.collide(S.kind, ph)
+    lp.steps(S.kind, ph, prog, max(3, args.warmup))
     torch.cuda.synchronize()
     clocks = Clocks(local)
     clocks.start()
@@ -363,7 +495,7 @@ def main():
     _, l0 = lp.stats()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    lp.steps(A.AD_NATURAL, ph, prog, args.steps)
+    lp.steps(S.kind, ph, prog, args.steps)
     e1.record(stream)
     torch.cuda.synchronize()
     if dist:
@@ -376,17 +508,17 @@ def main():
     ms_step = tmax / args.steps
 
     # end to end through the C ABI with pinned host buffers
-    ha = torch.from_numpy(alpha).pin_memory()
-    hk = torch.from_numpy(kappa).pin_memory()
-    outs = [torch.empty(n, dtype=torch.float64).pin_memory() for _ in range(1 + wl["nd"])]
-    out_ids = [A.TEM, A.UX, A.UY] + ([A.UZ] if wl["nd"] == 3 else [])
+    ha = torch.from_numpy(S.fields[A.ALPHA]).pin_memory()
+    hk = torch.from_numpy(S.fields[A.KAPPA]).pin_memory()
+    outs = [torch.empty(n, dtype=torch.float64).pin_memory() for _ in range(1 + S.nd)]
+    out_ids = [A.TEM, A.UX, A.UY] + ([A.UZ] if S.nd == 3 else [])
     interval = 100
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(args.e2e_steps):
         lp.set_field_ptr(A.ALPHA, ha.data_ptr())
         lp.set_field_ptr(A.KAPPA, hk.data_ptr())
-        lp.solve(A.AD_NATURAL, ph, prog, max_steps=interval, check_every=interval, tol=0.0)
+        lp.solve(S.kind, ph, prog, max_steps=interval, check_every=interval, tol=0.0)
         for fid, buf in zip(out_ids, outs):
             lp.get_field_ptr(fid, buf.data_ptr())
     torch.cuda.synchronize()
@@ -394,8 +526,8 @@ def main():
     e2e = {"value": n * interval / e2e_s / 1e6, "unit": "MLUPS", "h2d_bytes_per_step": 2 * n * 8,
            "d2h_bytes_per_step": len(outs) * n * 8, "time_steps_per_call": interval}
 
-    bpn = bytes_per_node(q, wl["storage"])
-    pop_mb = 2 * q * n * {"fp64": 8, "fp32": 4, "fp16": 2, "bf16": 2}[wl["storage"]] / 1e6
+    bpn = S.bytes_per_node()
+    pop_mb = 2 * q * n * {"fp64": 8, "fp32": 4, "fp16": 2, "bf16": 2}[S.storage] / 1e6
     peak, src = peaks()
     achieved = n * bpn / (ms_step / 1e3) / 1e9
     tpn = traffic_per_node(args.workload)
@@ -404,49 +536,23 @@ def main():
             "traffic": (tpn * n if tpn else None), "kernel": "fused step (interior + boundary kernels)"}
     line = {"metric": METRIC, "value": round(value, 1), "unit": "MLUPS", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms_step, 5), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32" if wl["storage"] != "fp64" else "f64",
+            "vs_baseline": None, "dtype": "f32" if S.storage != "fp64" else "f64",
             "data": "synthetic (seeded GRF design, correlation length 8)",
-            "config": {"workload": args.workload, "nodes": n, "storage": wl["storage"], "parallelism": "replicas",
+            "config": {"workload": args.workload, "nodes": n, "storage": S.storage, "parallelism": "replicas",
                        "l2": "inputs larger than L2: two population buffers of %.0f MB each" % pop_mb},
             "roofline": roof, "e2e": e2e, "clocks": ck, "gpu_launches": int(l1 - l0)}
+    lp.close()
     if rank == 0 and not args.no_design:
-        dp, _, r = design_gpu()
-        di = {"lattice": "heatsink2d-200x100-fp64", "tol": 1e-6, "max_steps": 100000,
-              "seconds": round(r["seconds"]["total"], 4),
-              "phases_s": {k: round(v, 4) for k, v in r["seconds"].items()},
-              "forward_steps": r["forward"][1], "adjoint_steps": r["adjoint"][1],
-              "converged": [r["forward"][0] == A.PL_CONVERGED, r["adjoint"][0] == A.PL_CONVERGED],
-              "objective": r["objective"],
-              "what": "filter, forward and adjoint to residual 1e-6 (checked every 100 steps), heat-source "
-                      "sensitivity, filtered and normalised sensitivity; from rest; no MMA update"}
-        if not args.no_cpu:
-            cs = design_cpu_per_step(dp)
-            di["cpu_seconds_est"] = round(cs["forward"] * r["forward"][1] + cs["adjoint"] * r["adjoint"][1], 2)
-            di["cpu_sample"] = ("oracle port, FP64, %d host threads: %d forward and %d adjoint steps timed, scaled to the "
-                                "GPU's step counts" % (os.cpu_count() or 1, cs["forward_sample"], cs["adjoint_sample"]))
-        line["design_iter"] = di
-    if rank == 0 and not args.no_design:
-        try:
-            line["design_iter_3d"] = design_gpu_3d()
-        except Exception as e:   # reported, not fatal
-            line["design_iter_3d"] = {"error": str(e)[:300]}
+        leg(line, "config1_cavity", cavity_leg) if not args.no_cpu else None
+        leg(line, "design_iter", design_leg, cpu=not args.no_cpu)
+        leg(line, "design_iter_3d_surrogate", surrogate_leg)
+        leg(line, "precision_errors", precision_leg)
     if rank == 0 and not args.no_transient:
-        try:
-            line["transient_iter"] = transient_gpu()
-        except Exception as e:   # reported, not fatal: the step throughput above stands on its own
-            line["transient_iter"] = {"error": str(e)[:300]}
+        leg(line, "transient_iter", transient_gpu)
     if rank == 0 and not args.no_cpu:
-        line["cpu_baseline"] = cpu_port(p, alpha, kappa, ops, q)
-        ti = line.get("transient_iter", {})
-        if "seconds" in ti and line["cpu_baseline"].get("value"):
-            d = TRANSIENT_LATTICE
-            nodes = d["lx"] * d["ly"] * d["lz"]
-            ti["cpu_seconds_est"] = round(2 * (d["levels"] - 1) * nodes / (line["cpu_baseline"]["value"] * 1e6), 1)
-            ti["cpu_sample"] = ("the cpu_baseline step rate (oracle port, FP64, all host threads) applied to the "
-                                "forward and adjoint steps, without recomputation")
+        line["cpu_baseline"] = cpu_port(S)
     if rank == 0:
         print(json.dumps(line), flush=True)
-    lp.close()
     if dist:
         dist.destroy_process_group()
 

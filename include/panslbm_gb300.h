@@ -207,7 +207,9 @@ int pl_program_destroy(pl_lattice h, int prog);
 
 /* initial conditions: which 0 NS::InitialCondition(rho,u), 1 AD::(T,u), 2 ANS::(u; ip,iu),
  * 3 AAD::(u; iT,iq), 4 NSin::(rho,u), 5 ANSin::(ip,iu) (D2Q9; ux, uy may be NULL).
- * a0..a3 = the scalar/vector inputs, ux..uz = the velocity argument. */
+ * a0..a3 = the scalar/vector inputs, ux..uz = the velocity argument. For the adjoint seeds (2, 3)
+ * ux = uy = uz = NULL takes the frozen forward velocity already on the device (pl_freeze_forward)
+ * and a0 = NULL a zero adjoint state, so an adjoint solve starts without host traffic. */
 int pl_init(pl_lattice h, int which, const double *a0, const double *a1, const double *a2, const double *a3,
             const double *ux, const double *uy, const double *uz);
 
@@ -361,6 +363,10 @@ int pl_unet_gradients(pl_unet u, float *host);
 int pl_unet_dataset_reserve(pl_unet u, int nsamples, int targets);
 int pl_unet_set_static(pl_unet u, const float *feat, int nfeat);
 int pl_unet_add_sample(pl_unet u, int slot, const double *design, const double *targets);
+/* the same from a lattice's device fields, without host traffic: targets = the frozen forward
+ * solution (rho - 1, ux, uy, uz, T) and the last saved adjoint macros (ip, iux, iuy, iuz, iT,
+ * iqx, iqy, iqz) of lattice h (same node count) */
+int pl_unet_add_sample_lattice(pl_unet u, int slot, const double *design, pl_lattice h);
 /* train on samples 0..nsamples-1 (targets normalised per channel over them) for `epochs`
  * shuffled passes of mini-batches; loss_per_epoch (may be NULL) receives the mean squared error
  * of the normalised targets per epoch */

@@ -67,7 +67,7 @@ EXPORTS = [
     "pl_mma_update", "pl_mma_destroy", "pl_mma_get_state", "pl_mma_set_state", "pl_debug_fail_alloc",
     "pl_unet_create", "pl_unet_destroy", "pl_unet_param_count", "pl_unet_init_params", "pl_unet_get_params",
     "pl_unet_set_params", "pl_unet_forward", "pl_unet_backward", "pl_unet_gradients", "pl_unet_dataset_reserve",
-    "pl_unet_set_static", "pl_unet_add_sample", "pl_unet_train", "pl_unet_set_norm", "pl_unet_get_norm",
+    "pl_unet_set_static", "pl_unet_add_sample", "pl_unet_add_sample_lattice", "pl_unet_train", "pl_unet_set_norm", "pl_unet_get_norm",
     "pl_unet_predict",
 ]
 

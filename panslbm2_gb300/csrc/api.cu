@@ -807,6 +807,20 @@ int scratch(pl_lattice h, int i, double **p) {
 // ==================================================================================== C ABI
 int pl::record_error(int code, const char *msg) { return fail(code, "%s", msg); }
 
+int pl::lattice_sample_fields(pl_lattice h, const double **p, long long *n) {
+    if (!h || !p || !n) return fail(PL_ERR_ARG, "bad arguments");
+    static const int fwd[5] = {PL_FWD_RHO, PL_FWD_UX, PL_FWD_UY, PL_FWD_UZ, PL_FWD_TEM};
+    for (int m = 0; m < 5; ++m) p[m] = h->fld[fwd[m]];
+    static const int adj[8] = {0, 1, 2, 3, 7, 8, 9, 10};   // ip, iu, iT, iq in the adjoint macro planes
+    for (int m = 0; m < 8; ++m) p[5 + m] = h->adj_saved >= 0 ? h->adj[h->adj_saved][adj[m]] : nullptr;
+    if (!p[0] || !p[4]) return fail(PL_ERR_STATE, "no frozen forward solution (pl_freeze_forward)");
+    if (h->adj_saved < 0) return fail(PL_ERR_STATE, "no saved adjoint collide");
+    *n = h->n;
+    return PL_OK;
+}
+
+cudaStream_t pl::lattice_stream(pl_lattice h) { return h ? h->st : nullptr; }
+
 extern "C" {
 
 const char *pl_last_error(void) { return g_err.c_str(); }
@@ -1078,11 +1092,17 @@ int pl_program_destroy(pl_lattice h, int prog) {
 int pl_init(pl_lattice h, int which, const double *a0, const double *a1, const double *a2, const double *a3,
             const double *ux, const double *uy, const double *uz) {
     PL_RANGE("pl_init");
-    if (!h || which < 0 || which > 5 || !a0) return fail(PL_ERR_ARG, "bad arguments");
+    const bool adj_seed = which == 2 || which == 3;
+    if (!h || which < 0 || which > 5 || (!a0 && !adj_seed)) return fail(PL_ERR_ARG, "bad arguments");
     if (which >= 4 && h->nd != 2) return fail(PL_ERR_UNSUPPORTED, "init %d is D2Q9 only", which);
-    if (which != 5 && (!ux || !uy || (h->nd == 3 && !uz))) return fail(PL_ERR_ARG, "init %d needs the velocity", which);
-    if ((which == 2 || which == 3 || which == 5) && (!a1 || !a2 || (h->nd == 3 && !a3)))
-        return fail(PL_ERR_ARG, "adjoint init needs a1..a3");
+    // the adjoint seeds may take the frozen forward velocity on the device (ux == NULL) and a zero
+    // adjoint state (a0..a3 == NULL), so that an adjoint solve starts without host traffic
+    const bool dev_u = adj_seed && !ux && !uy && !uz;
+    if (dev_u && (!h->fld[PL_FWD_UX] || !h->fld[PL_FWD_UY] || (h->nd == 3 && !h->fld[PL_FWD_UZ])))
+        return fail(PL_ERR_STATE, "init %d without a velocity needs the frozen forward solution", which);
+    if (which != 5 && !dev_u && (!ux || !uy || (h->nd == 3 && !uz))) return fail(PL_ERR_ARG, "init %d needs the velocity", which);
+    if (which == 5 && (!a1 || !a2)) return fail(PL_ERR_ARG, "adjoint init needs a1..a3");
+    if (adj_seed && a0 && (!a1 || !a2 || (h->nd == 3 && !a3))) return fail(PL_ERR_ARG, "adjoint init needs a1..a3");
     double *buf;
     int r = scratch(h, 1, &buf);   // q*N doubles >= 7*N
     if (r) return r;
@@ -1090,9 +1110,13 @@ int pl_init(pl_lattice h, int which, const double *a0, const double *a1, const d
     const double *in[7];
     for (int m = 0; m < 7; ++m) {
         double *d = buf + (size_t)m * h->n;
+        in[m] = d;
+        if (dev_u && m >= 4 && m - 4 < h->nd) {
+            in[m] = h->fld[PL_FWD_UX + (m - 4)];   // device-resident forward velocity
+            continue;
+        }
         if (hs[m] && (m < 4 || m - 4 < h->nd)) { if ((r = upload(h, d, hs[m], h->n))) return r; }
         else { CK(cudaMemsetAsync(d, 0, sizeof(double) * h->n, h->st)); }
-        in[m] = d;
     }
     KArgs a;
     memset(&a, 0, sizeof a);

@@ -24,3 +24,11 @@ PL_DECL(d3q15_bf16)
 // records the message pl_last_error returns (for entry points defined outside api.cu)
 int record_error(int code, const char *msg);
 }  // namespace pl
+
+typedef struct pl_lattice_s *pl_lattice;
+namespace pl {
+// device pointers of a lattice's frozen forward solution (rho, ux, uy, uz, T) and last saved
+// adjoint macros (ip, iux, iuy, iuz, iT, iqx, iqy, iqz); unused planes are NULL
+int lattice_sample_fields(pl_lattice h, const double **p, long long *n);
+cudaStream_t lattice_stream(pl_lattice h);
+}  // namespace pl

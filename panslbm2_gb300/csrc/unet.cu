@@ -162,22 +162,26 @@ int mkbuf(pl_unet u, Buf &b, int C, int level) {
 }
 
 int round1k(int b) { return (b + 1023) & ~1023; }
+// unused shared memory after the barriers: operand descriptors address only the stage buffers,
+// and this margin keeps every address an MMA could form from a descriptor inside the CTA's
+// allocation
+constexpr int kSmemGuard = 16 * 1024;
 // stage buffers are 1024-byte aligned (the 128-byte swizzle atom), see k_conv
 int conv_stages(int ck, int n) {
     const int stage = round1k(128 * ck * 2) + round1k(n * ck * 2);
-    return std::max(2, std::min(8, (200 * 1024) / stage));
+    return std::max(2, std::min(8, (184 * 1024) / stage));
 }
 int conv_smem(int ck, int n) {
     const int S = conv_stages(ck, n);
-    return S * (round1k(128 * ck * 2) + round1k(n * ck * 2)) + 1024 + (2 * S + 1) * 8 + 16;
+    return S * (round1k(128 * ck * 2) + round1k(n * ck * 2)) + 1024 + (2 * S + 1) * 8 + 16 + kSmemGuard;
 }
 int wgrad_stages(int cout) {
     const int stage = 128 * 128 * 2 + 128 * cout * 2;
-    return std::max(2, std::min(6, (200 * 1024) / stage));
+    return std::max(2, std::min(6, (184 * 1024) / stage));
 }
 int wgrad_smem(int cout) {
     const int S = wgrad_stages(cout);
-    return S * (128 * 128 * 2 + 128 * cout * 2) + 1024 + (2 * S + 1) * 8 + 16;
+    return S * (128 * 128 * 2 + 128 * cout * 2) + 1024 + (2 * S + 1) * 8 + 16 + kSmemGuard;
 }
 
 // one implicit-GEMM convolution: in (map mA, chunk ck, K channels cin) x weights (map mB) ->
@@ -635,6 +639,28 @@ int pl_unet_add_sample(pl_unet u, int slot, const double *design, const double *
     UCK(cudaMemcpyAsync(u->ds_design + slot * V0, d.data(), sizeof(float) * V0, cudaMemcpyHostToDevice, u->st));
     UCK(cudaMemcpyAsync(u->ds_target + slot * V0 * u->cused, t.data(), sizeof(float) * V0 * u->cused,
                         cudaMemcpyHostToDevice, u->st));
+    UCK(cudaStreamSynchronize(u->st));
+    return PL_OK;
+}
+
+int pl_unet_add_sample_lattice(pl_unet u, int slot, const double *design, pl_lattice h) {
+    if (!u || !design || !h || slot < 0 || slot >= u->nds) return uerr(PL_ERR_ARG, "bad arguments");
+    const long long V0 = u->lev[0].V;
+    pl::unet::SampleSrc src;
+    memset(&src, 0, sizeof src);
+    long long n = 0;
+    int r = pl::lattice_sample_fields(h, src.f, &n);
+    if (r) return r;
+    if (n != V0) return uerr(PL_ERR_ARG, "lattice has %lld nodes, the network %lld voxels", n, V0);
+    if (u->cused > 13) return uerr(PL_ERR_ARG, "a lattice sample has 13 target fields");
+    // order the lattice's work before the copy: its stream finishes the solve first
+    UCK(cudaStreamSynchronize(pl::lattice_stream(h)));
+    std::vector<float> d(V0);
+    for (long long v = 0; v < V0; ++v) d[v] = float(design[v]);
+    UCK(cudaMemcpyAsync(u->ds_design + slot * V0, d.data(), sizeof(float) * V0, cudaMemcpyHostToDevice, u->st));
+    pl::unet::k_capture<<<blocks_for(V0 * u->cused), 256, 0, u->st>>>(src, u->cused, V0,
+                                                                      u->ds_target + slot * V0 * u->cused);
+    UCK(cudaGetLastError());
     UCK(cudaStreamSynchronize(u->st));
     return PL_OK;
 }

@@ -520,6 +520,18 @@ __global__ void k_channel_stats(const float *raw, long long n, int cused, double
     }
 }
 
+// a training sample's targets from a lattice's FP64 device fields: out[v][c] = f_c[v] (rho - 1 for
+// c = 0), zero for a missing field
+struct SampleSrc { const double *f[16]; };
+__global__ void k_capture(SampleSrc src, int cused, long long nvox, float *out) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nvox * cused) return;
+    const int c = int(t % cused);
+    const long long v = t / cused;
+    const double *f = src.f[c];
+    out[t] = f ? float(f[v] - (c == 0 ? 1.0 : 0.0)) : 0.f;
+}
+
 // de-normalised prediction: out[c][v] = pred[v][c] * std[c] + mean[c] (c < cused), FP64
 __global__ void k_denorm(const float *pred, int C, int cused, const float *mean, const float *stdv, long long nvox,
                          double *out) {

@@ -244,15 +244,30 @@ class ForcedHeatSink:
             lp.init(1, seed["tem"], ux=seed["ux"], uy=seed["uy"], uz=uz)
 
     def seed_adjoint(self, fu, seed=None):
-        """ANS / AAD initial condition with the forward velocity fu: zero adjoint or predicted"""
+        """ANS / AAD initial condition with the forward velocity: zero adjoint (from the frozen
+        forward velocity on the device) or predicted"""
         lp, zero = self.lp, np.zeros(self.n)
         if seed is None:
-            lp.init(2, zero, zero, zero, zero, ux=fu[0], uy=fu[1], uz=fu[2])
-            lp.init(3, zero, zero, zero, zero, ux=fu[0], uy=fu[1], uz=fu[2])
+            lp.init(2, None)
+            lp.init(3, None)
         else:
             g = lambda k: seed.get(k, zero)  # noqa: E731
             lp.init(2, g("ip"), g("iux"), g("iuy"), g("iuz"), ux=fu[0], uy=fu[1], uz=fu[2])
             lp.init(3, g("item"), g("iqx"), g("iqy"), g("iqz"), ux=fu[0], uy=fu[1], uz=fu[2])
+
+    def solve_pair(self, s, tol=1e-6, max_steps=100000, max_adjoint_steps=None, check_every=100):
+        """forward and adjoint solves of design s from rest, leaving both solutions on the device
+        (for a training sample); returns the filtered design and the (status, steps) of both"""
+        lp = self.lp
+        ss = self.filtered(s)
+        self.set_design(ss)
+        self.seed_forward(None)
+        st_f, nf, _ = lp.solve(A.AD_FORCE, self.ph, self.prog_f, max_steps, check_every, tol)
+        lp.freeze_forward()
+        self.seed_adjoint(None)
+        st_a, na, _ = lp.solve(A.AAD_FORCE, self.ph, self.prog_a, max_adjoint_steps or max_steps, check_every, tol)
+        lp.synchronize()
+        return ss, (st_f, nf), (st_a, na)
 
     def iterate(self, s, tol=1e-6, max_steps=100000, check_every=100, seed=None, filtered=None,
                 fixed_steps=None):

@@ -118,6 +118,11 @@ class UNet:
         feat = np.ascontiguousarray(feat, np.float32)
         check(self.lib.pl_unet_set_static(self.h, _fp(feat), feat.shape[1]))
 
+    def add_sample_lattice(self, slot, design, lattice):
+        """targets from the lattice's frozen forward and saved adjoint fields, device to device"""
+        design = np.ascontiguousarray(design, np.float64)
+        check(self.lib.pl_unet_add_sample_lattice(self.h, slot, design.ctypes.data_as(A.DP), lattice.h))
+
     def add_sample(self, slot, design, targets):
         design = np.ascontiguousarray(design, np.float64)
         targets = np.ascontiguousarray(targets, np.float64)
@@ -205,21 +210,26 @@ class SurrogateWarmStart:
         self.hs.close()
         self.net.close()
 
-    def generate(self, seeds, tol=1e-6, max_steps=100000, log=None):
-        """solve each seeded design to `tol`; store the pairs; returns per-sample step counts"""
-        self.net.reserve(len(seeds))
-        info = []
-        for slot, sd in enumerate(seeds):
+    def generate(self, count, first_seed=1000, tol=1e-6, max_steps=100000, max_adjoint_steps=40000, log=None):
+        """solve seeded designs first_seed, first_seed + 1, ... to `tol` until `count` pairs whose
+        forward and adjoint both converged are stored (the others are skipped and logged);
+        returns the per-design records"""
+        self.net.reserve(count)
+        info, slot, sd = [], 0, first_seed
+        while slot < count:
             t0 = time.perf_counter()
             s = self.p.design(seed=sd)
-            r = self.hs.iterate(s, tol=tol, max_steps=max_steps)
-            self.net.add_sample(slot, r["ss"], targets_of(r))
-            rec = dict(seed=int(sd), forward=r["forward"][1], adjoint=r["adjoint"][1],
-                       converged=[r["forward"][0] == A.PL_CONVERGED, r["adjoint"][0] == A.PL_CONVERGED],
+            ss, (stf, nf), (sta, na) = self.hs.solve_pair(s, tol, max_steps, max_adjoint_steps)
+            ok = stf == A.PL_CONVERGED and sta == A.PL_CONVERGED
+            if ok:
+                self.net.add_sample_lattice(slot, ss, self.hs.lp)
+                slot += 1
+            rec = dict(seed=int(sd), forward=nf, adjoint=na, status=[int(stf), int(sta)], used=ok,
                        seconds=round(time.perf_counter() - t0, 3))
             info.append(rec)
             if log:
                 log(rec)
+            sd += 1
         return info
 
     def train(self, nsamples, epochs, batch=1, lr=1e-3, seed=0):
@@ -274,23 +284,27 @@ def main(argv=None):
     p = ForcedParams(3, nx, ny, nz)
     sw = SurrogateWarmStart(p, "fp32", a.levels, a.base, a.batch)
     rec = dict(shape=[nx, ny, nz], nsamples=a.nsamples, epochs=a.epochs, batch=a.batch, lr=a.lr,
-               seeds=[a.first_seed, a.first_seed + a.nsamples - 1], params=sw.net.nparam)
+               first_seed=a.first_seed, params=sw.net.nparam)
     log = []
 
     def out(d):
         print(json.dumps(d), flush=True)
 
     t0 = time.perf_counter()
-    rec["samples"] = sw.generate(range(a.first_seed, a.first_seed + a.nsamples), tol=a.data_tol or a.tol,
+    rec["samples"] = sw.generate(a.nsamples, a.first_seed, tol=a.data_tol or a.tol,
                                  log=lambda d: (log.append(d), out(dict(sample=d))))
     rec["generate_s"] = round(time.perf_counter() - t0, 2)
+    used = [d["seed"] for d in rec["samples"] if d["used"]]
+    rec["seeds"] = [min(used), max(used)]
+    rec["skipped_seeds"] = [d["seed"] for d in rec["samples"] if not d["used"]]
     t1 = time.perf_counter()
     loss = sw.train(a.nsamples, a.epochs, a.batch, a.lr, seed=7)
     sw.hs.lp.synchronize()
     rec["train_s"] = round(time.perf_counter() - t1, 2)
     rec["loss"] = [float(v) for v in loss]
     out(dict(loss=rec["loss"], train_s=rec["train_s"]))
-    sw.net.save(a.out, meta=dict(nsamples=a.nsamples, epochs=a.epochs, seeds=rec["seeds"]))
+    sw.net.save(a.out, meta=dict(nsamples=a.nsamples, epochs=a.epochs, seeds=rec["seeds"],
+                                 skipped=rec["skipped_seeds"], data_tol=a.data_tol or a.tol))
     s = p.design(seed=a.eval_seed)
     ev = {}
     for name, warm in (("plain", False), ("surrogate", True), ("plain_again", False), ("surrogate_again", True)):

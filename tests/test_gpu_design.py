@@ -35,5 +35,6 @@ def test_adjoint_sensitivity_matches_finite_differences():
         ratios.append(r0["dfdss"][idx] / fd)
     hs.close()
     ratios = np.array(ratios)
+    print("adjoint / FD ratios", ratios.tolist(), "source length L", p.L)
     assert np.all(ratios > 0)
     assert np.max(np.abs(ratios / ratios.mean() - 1.0)) < 0.02, ratios
