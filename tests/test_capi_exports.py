@@ -16,7 +16,7 @@ def declared():
     for f in os.listdir(os.path.join(ROOT, "include")):
         if f.endswith(".h"):
             src = open(os.path.join(ROOT, "include", f)).read()
-            names += re.findall(r"^\s*(?:int|const char \*|double)\s*\*?\s*(pl_\w+)\s*\(", src, flags=re.M)
+            names += re.findall(r"^\s*(?:int|long long|const char \*|double)\s*\*?\s*(pl_\w+)\s*\(", src, flags=re.M)
     return sorted(set(names))
 
 
