@@ -19,7 +19,16 @@ state of step t, the sensitivity term of step t (forward snapshot gi[t], adjoint
 then iStream and the adjoint boundary calls with the velocity of step t. The reference's forward
 loop never writes gi[0], which its adjoint reads at t = 0 (allocated but not initialised); here
 that snapshot is zero.
+
+The same sweep runs the forced-convection heat sink of panslbm2_gb300.forced (the transient
+benchmark configuration): AD / AAD ForceConvection kinds with the volumetric heat source, the
+time-varying inflow u(t) = u_max (1 - exp(-t / tau_in)) through pl_set_inflow_scale (NS SetU of
+forward step t and ANS iSetU of adjoint step t use u(t)), the time-averaged objective
+J = (1 / nt) sum_t sum_x w(x) T_t(x) entering each adjoint collide as the objective weight w / nt,
+and per step the Brinkman and diffusivity terms (AAD::SensitivityBrinkmanDiffusivity) plus, in 2D,
+the heat-source term.
 """
+import math
 import time
 
 import numpy as np
@@ -30,15 +39,38 @@ from .lattice import LatticePair, phys
 
 
 class TransientHeatSink:
-    def __init__(self, p, storage="fp64", checkpoint_every=100):
+    """p: heatsink.Params (natural convection, the reference's transient driver) or
+    forced.ForcedParams (forced convection with the time-varying inflow, time constant tau_in)"""
+
+    def __init__(self, p, storage="fp64", checkpoint_every=100, tau_in=500.0):
+        from .forced import ForcedParams
         self.p, self.K = p, int(checkpoint_every)
+        self.forced = isinstance(p, ForcedParams)
         self.q = 9 if p.nd == 2 else 15
         self.n = p.lx * p.ly * p.lz
         self.lp = LatticePair(self.q, p.lx, p.ly, p.lz, storage)
-        self.prog_f = self.lp.program(HS.to_descs(HS.program_ops("forward", p)))
-        self.prog_a = self.lp.program(HS.to_descs(HS.program_ops("adjoint", p)))
-        self.ph = phys(nu=p.nu, diff=0.0, gx=p.gx, gy=p.gy, gz=p.gz, tem0=p.tem0)
-        self.qn, self.mask = p.source()
+        if self.forced:
+            self.kf, self.ka = A.AD_FORCE, A.AAD_FORCE
+            self.prog_f = self.lp.program(HS.to_descs(p.program_ops("forward")))
+            self.prog_a = self.lp.program(HS.to_descs(p.program_ops("adjoint")))
+            self.ph = phys(nu=p.nu)
+            self.tau_in = float(tau_in)
+        else:
+            self.kf, self.ka = A.AD_NATURAL, A.AAD_NATURAL
+            self.prog_f = self.lp.program(HS.to_descs(HS.program_ops("forward", p)))
+            self.prog_a = self.lp.program(HS.to_descs(HS.program_ops("adjoint", p)))
+            self.ph = phys(nu=p.nu, diff=0.0, gx=p.gx, gy=p.gy, gz=p.gz, tem0=p.tem0)
+            self.qn, self.mask = p.source()
+
+    def inflow(self, t):
+        """u(t) / u_max of forward time level t (forced convection; 1 otherwise)"""
+        if not self.forced:
+            return 1.0
+        return 1.0 - math.exp(-t / self.tau_in)
+
+    def _bc_scale(self, t):
+        if self.forced:
+            self.lp.set_inflow_scale(self.inflow(t))
 
     def close(self):
         self.lp.close()
@@ -51,17 +83,31 @@ class TransientHeatSink:
         t0 = seg * self.K + 1
         for t in range(t0, t_last + 1):
             if t == t0:
-                lp.collide(A.AD_NATURAL, ph, save=True)
+                lp.collide(self.kf, ph, save=True)
             else:
-                lp.step(A.AD_NATURAL, ph, self.prog_f, save=True)
+                self._bc_scale(t - 1)   # the boundary calls in this step close forward step t - 1
+                lp.step(self.kf, ph, self.prog_f, save=True)
             lp.snapshot(0, host=False)
             lp.store(A.STORE_FWD, t - t0)
             lp.swap_snapshot(t - t0)   # moved, not copied: each snapshot is read back once
 
+    def evaluate_design(self, ss, nt, release=True):
+        """forced convection: the sweep for the filtered design ss (design maps, heat source and
+        objective weight of forced.ForcedParams)"""
+        p = self.p
+        alpha, kappa, dads, dkds = p.design_fields(ss)
+        Q, dQ = p.heat_source(ss)
+        self.lp.set_field(A.HEAT_SOURCE, Q)
+        self.w = p.objective_weight(ss)
+        self.lp.set_field(A.OBJ_WEIGHT, self.w / nt)
+        self.dQ = dQ
+        return self.evaluate(alpha, kappa, dads, dkds, nt, release)
+
     def evaluate(self, alpha, kappa, dads, dkds, nt, release=True):
-        """objective (time-averaged temperature on the heat source), its sensitivity dfdss and
-        the phase times; nt counts the time levels 0..nt-1 as the reference's loops do. With
-        release=False the device stores stay allocated for the next evaluation."""
+        """objective (time-averaged temperature on the heat source; forced convection: time
+        average of sum w T), its sensitivity dfdss (the reference's sign convention) and the phase
+        times; nt counts the time levels 0..nt-1 as the reference's loops do. With release=False
+        the device stores stay allocated for the next evaluation."""
         lp, n, K, nd = self.lp, self.n, self.K, self.p.nd
         zero, one = np.zeros(n), np.ones(n)
         times = {}
@@ -77,12 +123,14 @@ class TransientHeatSink:
         for t in range(1, nt):
             if (t - 1) % K == 0:
                 if t > 1:
+                    self._bc_scale(t - 1)
                     lp.stream(mode=0, prog=self.prog_f, both=True)
                 lp.store(A.STORE_POPS, (t - 1) // K)
                 nseg += 1
-                lp.collide(A.AD_NATURAL, self.ph, save=True)
+                lp.collide(self.kf, self.ph, save=True)
             else:
-                lp.step(A.AD_NATURAL, self.ph, self.prog_f, save=True)
+                self._bc_scale(t - 1)
+                lp.step(self.kf, self.ph, self.prog_f, save=True)
             lp.accumulate(A.ACC, A.TEM)
         ul = [lp.get_field(A.UX), lp.get_field(A.UY), lp.get_field(A.UZ) if nd == 3 else zero]
         times["forward"] = time.perf_counter() - t0
@@ -109,18 +157,29 @@ class TransientHeatSink:
                                (A.FWD_TEM, zero)):
                     lp.set_field(fid, v)
                 lp.set_snapshot(0, np.zeros(n * self.q))
-            lp.collide(A.AAD_NATURAL, self.ph, save=True)
+            lp.collide(self.ka, self.ph, save=True)
             lp.snapshot(1, host=False)
-            if first:
+            if self.forced:
+                # AAD::SensitivityBrinkmanDiffusivity; in 2D the design-dependent heat source adds
+                # -item dQ/dss per step (dQ/dss = -q_h, uniform), in the reference's sign
+                lp.sensitivity_device(1, dads if first else None, dkds if first else None)
+                if nd == 2:
+                    lp.accumulate(A.DFDS, A.ITEM, -float(self.dQ[0]))
+            elif first:
                 lp.sensitivity_device(0, dads, dkds, self.qn, self.mask)
-                first = False
             else:
                 lp.sensitivity_device(0)
+            first = False
+            self._bc_scale(t)
             lp.stream(mode=1, prog=self.prog_a, both=True)
         dfdss = lp.get_field(A.DFDS)
         acc = lp.get_field(A.ACC)
         times["adjoint"] = time.perf_counter() - t1
         if release:
             lp.store_release()
-        objective = float(np.sum(acc[self.mask != 0])) / (self.p.L * nt)
+        if self.forced:
+            lp.set_inflow_scale(1.0)
+            objective = float(np.sum(self.w * acc)) / nt
+        else:
+            objective = float(np.sum(acc[self.mask != 0])) / (self.p.L * nt)
         return dict(objective=objective, dfdss=dfdss, times=times, segments=nseg)

@@ -52,3 +52,41 @@ def test_transient_checkpoints_leave_the_result_unchanged_3d():
     assert res[0]["objective"] == res[1]["objective"]
     assert np.array_equal(res[0]["dfdss"], res[1]["dfdss"])
     assert np.all(np.isfinite(res[0]["dfdss"])) and np.any(res[0]["dfdss"] != 0)
+
+
+def test_forced_transient_with_time_varying_inflow_matches_oracle():
+    """The forced-convection transient (volumetric source, objective weight, u(t) inflow on NS SetU
+    and ANS iSetU) on D2Q9, FP64, checkpoints every 4 levels, against the oracle's run keeping
+    every level; tau_in = 20 so the inflow ramps within the 30 levels."""
+    from oracle.olib import Oracle
+    from panslbm2_gb300 import forced as FC
+    from tests import _forced_oracle as FO
+    p = FC.ForcedParams(2, 24, 12)
+    ss = p.project(np.clip(p.design(seed=6, sigma=3.0), 0, 1))
+    tr = TransientHeatSink(p, "fp64", checkpoint_every=4, tau_in=20.0)
+    r = tr.evaluate_design(ss, 30)
+    tr.close()
+    o = Oracle("oracle")
+    o.set_threads(1)
+    ref = FO.forced_transient(o, p, ss, 30, tau_in=20.0)
+    assert abs(r["objective"] - ref["objective"]) <= 1e-12 * abs(ref["objective"])
+    close(r["dfdss"], ref["dfdss"], 1e-10)
+
+
+def test_forced_transient_fp32_objective_against_fp64_3d():
+    """The transient configuration's physics in 3D (base-plate source, u(t) inflow) on a small
+    D3Q15 lattice over 300 levels: the FP32 objective within 1e-4 relative of FP64, the FP32
+    sensitivity close to FP64, and checkpointing bit-neutral in FP32."""
+    from panslbm2_gb300 import forced as FC
+    p = FC.ForcedParams(3, 40, 24, 24, plate=(12, 2, 12))
+    ss = p.project(np.clip(p.design(seed=7, sigma=4.0), 0, 1))
+    out = {}
+    for st, every in (("fp64", 100), ("fp32", 100), ("fp32", 7)):
+        tr = TransientHeatSink(p, st, checkpoint_every=every, tau_in=100.0)
+        out[(st, every)] = tr.evaluate_design(ss, 300)
+        tr.close()
+    a, b = out[("fp32", 100)], out[("fp64", 100)]
+    assert abs(a["objective"] - b["objective"]) <= 1e-4 * abs(b["objective"])
+    assert np.linalg.norm(a["dfdss"] - b["dfdss"]) <= 1e-2 * np.linalg.norm(b["dfdss"])
+    assert a["objective"] == out[("fp32", 7)]["objective"]
+    assert np.array_equal(a["dfdss"], out[("fp32", 7)]["dfdss"])
