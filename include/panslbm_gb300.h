@@ -176,12 +176,18 @@ int pl_synchronize(pl_lattice h);
  * stream) instead of the lattice's own non-blocking stream */
 int pl_set_stream(pl_lattice h, void *stream);
 /* launch options (no counterpart in the reference, which has no launch policy):
- *  PL_OPT_GRAPHS         1: pl_steps replays a captured two-step CUDA graph; 0 (default):
+ *  PL_OPT_GRAPHS         1: pl_steps, and pl_solve between its residual checks, replay a
+ *                        captured two-step CUDA graph; 0 (default):
  *                        eager launches, which keep the boundary streams' priority
  *  PL_OPT_SIDE_PRIORITY  1 (default): the boundary chains run on high-priority streams; 0:
  *                        lowest priority */
 #define PL_OPT_GRAPHS 1
 #define PL_OPT_SIDE_PRIORITY 2
+/*  PL_OPT_STOCHASTIC_ROUNDING  16-bit storage only. 0 (default): the collide stores round to
+ *                        nearest; 1: they round stochastically (unbiased), so increments below half
+ *                        a 16-bit ulp -- a small source added every step -- still accumulate in
+ *                        expectation. Replayed graphs reuse their captured seeds. */
+#define PL_OPT_STOCHASTIC_ROUNDING 3
 int pl_set_option(pl_lattice h, int option, int value);
 /* time-varying inflow (no counterpart in the reference, whose inflows are constant): the
  * prescribed velocity of every NS SetU / ANS iSetU op is multiplied by `scale` in the steps that
@@ -368,8 +374,9 @@ int pl_unet_add_sample(pl_unet u, int slot, const double *design, const double *
  * iqx, iqy, iqz) of lattice h (same node count) */
 int pl_unet_add_sample_lattice(pl_unet u, int slot, const double *design, pl_lattice h);
 /* train on samples 0..nsamples-1 (targets normalised per channel over them) for `epochs`
- * shuffled passes of mini-batches; loss_per_epoch (may be NULL) receives the mean squared error
- * of the normalised targets per epoch */
+ * shuffled passes of mini-batches, Adam with a cosine-decaying learning rate (lr down to lr/20);
+ * loss_per_epoch (may be NULL) receives the mean squared error of the normalised targets per
+ * epoch */
 int pl_unet_train(pl_unet u, int nsamples, int epochs, int batch, double lr, unsigned long long seed,
                   double *loss_per_epoch);
 /* the target normalisation (mean, std per target channel), e.g. to restore a trained model */
@@ -377,6 +384,11 @@ int pl_unet_set_norm(pl_unet u, const float *mean, const float *stdv);
 int pl_unet_get_norm(pl_unet u, float *mean, float *stdv);
 /* prediction for one design: out [targets][nvox] (de-normalised, FP64) */
 int pl_unet_predict(pl_unet u, const double *design, double *out);
+
+/* FP64 fused multiply-add throughput of the current device in TFLOP/s (2 flops per FMA), from a
+ * short kernel of independent FMA chains: the roofline denominator of the FP64 collide kinds (no
+ * counterpart in the reference) */
+int pl_probe_fp64_fma(double *tflops);
 
 /* last step kernel time (ms) measured with CUDA events on the lattice stream, and number
  * of kernels launched since creation */

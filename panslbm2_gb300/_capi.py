@@ -28,7 +28,7 @@ BC_EL_STRESS, BC_AEL_STRESS = 15, 16
 SMOOTH_CORNER, SMOOTH_AT, SMOOTH_LINE = 20, 21, 22
 # fields
 ALPHA, KAPPA, BETA, DIRX, DIRY, DIRZ, DENSITY, GAMMA = 0, 1, 2, 3, 4, 5, 6, 7
-OPT_GRAPHS, OPT_SIDE_PRIORITY = 1, 2
+OPT_GRAPHS, OPT_SIDE_PRIORITY, OPT_STOCHASTIC_ROUNDING = 1, 2, 3
 RHO, UX, UY, UZ, TEM, QX, QY, QZ = 8, 9, 10, 11, 12, 13, 14, 15
 IP, IUX, IUY, IUZ, IMX, IMY, IMZ, ITEM, IQX, IQY, IQZ = 16, 17, 18, 19, 20, 21, 22, 23, 24, 25, 26
 FWD_RHO, FWD_UX, FWD_UY, FWD_UZ, FWD_TEM = 32, 33, 34, 35, 36
@@ -68,7 +68,7 @@ EXPORTS = [
     "pl_unet_create", "pl_unet_destroy", "pl_unet_param_count", "pl_unet_init_params", "pl_unet_get_params",
     "pl_unet_set_params", "pl_unet_forward", "pl_unet_backward", "pl_unet_gradients", "pl_unet_dataset_reserve",
     "pl_unet_set_static", "pl_unet_add_sample", "pl_unet_add_sample_lattice", "pl_unet_train", "pl_unet_set_norm", "pl_unet_get_norm",
-    "pl_unet_predict",
+    "pl_unet_predict", "pl_probe_fp64_fma",
 ]
 
 _lib = None

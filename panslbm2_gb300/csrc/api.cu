@@ -138,6 +138,8 @@ struct pl_lattice_s {
     std::vector<char> snap_filled;   // PL_STORE_SNAP slots that hold a snapshot
     int *sens_mask = nullptr;        // source mask of pl_sensitivity_device
     double uscale = 1.0;             // pl_set_inflow_scale
+    bool sr = false;                 // PL_OPT_STOCHASTIC_ROUNDING
+    uint32_t sr_count = 0;           // launches so far (seeds the stochastic rounding)
 };
 
 namespace {
@@ -570,6 +572,8 @@ int build_args(pl_lattice h, int kind, const pl_phys *ph, int prog, int src, int
     a.save = save ? 1 : 0;
     a.err = h->err;
     a.uscale = h->uscale;
+    a.sr = (h->sr && h->ssize == 2) ? 1 : 0;
+    a.sr_seed = 0x9E3779B9u * (++h->sr_count);
     const bool adjk = pl::kind_is_adjoint(kind);
     const bool elk = pl::kind_elastic(kind);
     a.sgn = adjk ? 1 : -1;
@@ -942,6 +946,12 @@ int pl_set_option(pl_lattice h, int option, int value) {
         h->use_graphs = value == 1;
         return PL_OK;
     }
+    if (option == PL_OPT_STOCHASTIC_ROUNDING) {
+        h->sr = value == 1;
+        for (auto &kv : h->graphs) cudaGraphExecDestroy(kv.second.exec);
+        h->graphs.clear();
+        return PL_OK;
+    }
     if (option == PL_OPT_SIDE_PRIORITY) {
         const int prio = value ? h->prio_hi : h->prio_lo;
         if (prio == h->side_prio) return PL_OK;
@@ -1169,10 +1179,7 @@ int pl_step(pl_lattice h, int kind, const pl_phys *ph, int prog, int save) {
     return do_step(h, kind, ph, prog, save != 0);
 }
 
-int pl_steps(pl_lattice h, int kind, const pl_phys *ph, int prog, int n) {
-    PL_RANGE("pl_steps");
-    if (!h || !ph || n < 0) return fail(PL_ERR_ARG, "bad arguments");
-    CK(cudaEventRecord(h->ev0, h->st));
+static int run_steps(pl_lattice h, int kind, const pl_phys *ph, int prog, int n) {
     int r;
     // n fused steps without saves. Two steps return every buffer and slot to its parity, so
     // they are captured once into a CUDA graph and replayed (no per-kernel host launch cost).
@@ -1244,6 +1251,16 @@ int pl_steps(pl_lattice h, int kind, const pl_phys *ph, int prog, int n) {
     for (; done < n; ++done) {
         if ((r = do_step(h, kind, ph, prog, false))) return r;
     }
+    return PL_OK;
+}
+
+int pl_steps(pl_lattice h, int kind, const pl_phys *ph, int prog, int n) {
+    PL_RANGE("pl_steps");
+    if (!h || !ph || n < 0) return fail(PL_ERR_ARG, "bad arguments");
+    if (int e = check_kind(h, kind)) return e;
+    CK(cudaEventRecord(h->ev0, h->st));
+    int r = run_steps(h, kind, ph, prog, n);
+    if (r) return r;
     CK(cudaEventRecord(h->ev1, h->st));
     return PL_OK;
 }
@@ -1276,10 +1293,19 @@ int pl_solve(pl_lattice h, int kind, const pl_phys *ph, int prog, int max_steps,
     CK(cudaMemsetAsync(h->nonfinite, 0, sizeof(int), h->st));
     CK(cudaEventRecord(h->ev0, h->st));
     int r;
+    auto is_save = [&](int t) {
+        return (t % check_every == 0) || (t % check_every == check_every - 1) || check_every == 1;
+    };
     for (int t = 1; t <= max_steps; ++t) {
-        const bool save = (t % check_every == 0) || (t % check_every == check_every - 1) || check_every == 1;
+        const bool save = is_save(t);
         if (t == 1) r = do_collide(h, kind, ph, true);
-        else r = do_step(h, kind, ph, prog, save);
+        else if (!save && h->use_graphs) {
+            // the steps up to the next saving one replay the captured two-step graph
+            int t1 = t;
+            while (t1 < max_steps && !is_save(t1 + 1)) ++t1;
+            r = run_steps(h, kind, ph, prog, t1 - t + 1);
+            t = t1;
+        } else r = do_step(h, kind, ph, prog, save);
         if (r) return r;
         if (t % check_every == 0 && t > 1) {
             if ((r = residual_family(h, fa, r0, false))) return r;

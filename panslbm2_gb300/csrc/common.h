@@ -114,6 +114,8 @@ struct KArgs {
     // weight objw (dJ/dT) to every adjoint g population
     const void *hsrc, *objw;
     double uscale;              // factor on the prescribed velocity of NS SetU / ANS iSetU ops
+    int sr;                     // 16-bit storage: stochastic rounding of the collide's stores
+    uint32_t sr_seed;           // per-launch seed of the stochastic rounding
     double *out[11];            // macro outputs (forward: rho,ux,uy,uz,tem,qx,qy,qz;
                                 //  adjoint: ip,iux,iuy,iuz,imx,imy,imz,item,iqx,iqy,iqz;
                                 //  EL: ux,uy in 1,2 and sxx,sxy,syx,syy in 4..7;

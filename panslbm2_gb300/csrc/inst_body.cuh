@@ -53,7 +53,7 @@ static __device__ __forceinline__ void finish_boundary(int kind, TC *f, TC *g, i
         if (PL_LAT::ND == 3) a.bcu_out[2][node] = double(u[2]);
     }
     const TC sf = TC(a.ph.shift_f), sg = TC(a.ph.shift_g);
-    store_node<PL_LAT, PL_STORE, true>(static_cast<PL_STORE *>(a.dst), a.geo, node, f, g, sf, sg);
+    store_collided<PL_LAT, PL_STORE, true>(a, node, f, g, sf, sg);
     (void)Q;
 }
 

@@ -66,6 +66,28 @@ __device__ __forceinline__ void store_node(S *__restrict__ dst, const Geo &g, in
     }
 }
 
+// the collide's store with stochastic rounding for 16-bit storage when a.sr is set
+template <class L, class S, bool HAS_G>
+__device__ __forceinline__ void store_collided(const KArgs &a, int idx, const typename Store<S>::T *f,
+                                               const typename Store<S>::T *gg, typename Store<S>::T sf,
+                                               typename Store<S>::T sg) {
+    using T = typename Store<S>::T;
+    constexpr bool SIXTEEN = sizeof(S) == 2;
+    if (!SIXTEEN || !a.sr) {
+        store_node<L, S, HAS_G>(static_cast<S *>(a.dst), a.geo, idx, f, gg, sf, sg);
+        return;
+    }
+    constexpr int Q = L::Q;
+    S *dst = static_cast<S *>(a.dst);
+    uint32_t st = sr_hash(uint32_t(idx), a.sr_seed);
+#pragma unroll
+    for (int c = 0; c < Q; ++c) {
+        const uint32_t r = sr_next(st);
+        dst[(long long)c * a.geo.np + idx] = StoreSR<S>::enc(f[c], L::template w<T>(c) * sf, r);
+        if (HAS_G) dst[(long long)(Q + c) * a.geo.np + idx] = StoreSR<S>::enc(gg[c], L::template w<T>(c) * sg, r >> 16);
+    }
+}
+
 // ---- interior kernel --------------------------------------------------------------------
 // PULL: stream + boundary program (fused step); otherwise collide in place. With a staged
 // boundary program (a.icode), nodes on a face or flagged carry a code: -2 = handled by the
@@ -108,7 +130,7 @@ __device__ __forceinline__ void node_tail(const KArgs &a, int idx, int code, typ
             if (L::ND == 3) a.bcu_out[2][idx] = double(u[2]);
         }
     }
-    store_node<L, S, HG>(static_cast<S *>(a.dst), a.geo, idx, f, g, sf, sg);
+    store_collided<L, S, HG>(a, idx, f, g, sf, sg);
 }
 
 // Launched on a (ceil(nx/32), ceil(ny/8), nz) grid of 32 x 8 blocks: lane = x within a 32-node
@@ -215,7 +237,7 @@ __global__ void __launch_bounds__(128) k_boundary(KArgs a) {
         if (L::ND == 3) a.bcu_out[2][idx] = double(u[2]);
     }
     const T sf = T(a.ph.shift_f), sg = T(a.ph.shift_g);
-    store_node<L, S, HG>(static_cast<S *>(a.dst), a.geo, idx, f, g, sf, sg);
+    store_collided<L, S, HG>(a, idx, f, g, sf, sg);
 }
 
 // ---- staged boundary path -------------------------------------------------------------------

@@ -102,4 +102,45 @@ template <> struct Store<__nv_bfloat16> {
     __device__ __forceinline__ static __nv_bfloat16 enc(float v, float shift) { return __float2bfloat16_rn(v - shift); }
 };
 
+// ---- stochastic rounding of 16-bit stores ----------------------------------------------------
+// Round-to-nearest discards every increment below half a 16-bit ulp, so a small source added each
+// step (a heat source of 1e-3 on temperatures of order 1) never accumulates. Rounding up with
+// probability (x - lo) / (hi - lo) keeps the expected stored value equal to x. r: 16 random bits.
+// Other storage types round to nearest.
+template <class S> struct StoreSR {
+    __device__ __forceinline__ static S enc(typename Store<S>::T v, typename Store<S>::T shift, uint32_t) {
+        return Store<S>::enc(v, shift);
+    }
+};
+template <> struct StoreSR<__nv_bfloat16> {
+    __device__ __forceinline__ static __nv_bfloat16 enc(float v, float shift, uint32_t r) {
+        const float x = v - shift;
+        uint32_t b = __float_as_uint(x);
+        if ((b & 0x7f800000u) != 0x7f800000u) b += (r & 0xffffu);   // finite: add below the kept bits
+        return __ushort_as_bfloat16((unsigned short)(b >> 16));
+    }
+};
+template <> struct StoreSR<__half> {
+    __device__ __forceinline__ static __half enc(float v, float shift, uint32_t r) {
+        const float x = v - shift;
+        const __half lo = __float2half_rz(x);
+        const unsigned short lb = __half_as_ushort(lo);
+        if ((lb & 0x7c00u) == 0x7c00u) return lo;                      // inf / nan
+        const __half hi = __ushort_as_half((unsigned short)(lb + 1));  // next magnitude away from 0
+        const float flo = __half2float(lo), fhi = __half2float(hi);
+        const float p = (x - flo) / (fhi - flo);
+        return float(r & 0xffffu) * (1.0f / 65536.0f) < p ? hi : lo;
+    }
+};
+// per-node random stream: a hashed seed, then xorshift32 per value
+__device__ __forceinline__ uint32_t sr_hash(uint32_t a, uint32_t b) {
+    uint32_t h = a * 0x9E3779B1u ^ (b + 0x7F4A7C15u) * 0x85EBCA77u;
+    h ^= h >> 15; h *= 0x2C1B3C6Du; h ^= h >> 12; h *= 0x297A2D39u; h ^= h >> 15;
+    return h | 1u;
+}
+__device__ __forceinline__ uint32_t sr_next(uint32_t &s) {
+    s ^= s << 13; s ^= s >> 17; s ^= s << 5;
+    return s;
+}
+
 }  // namespace pl

@@ -718,6 +718,8 @@ int pl_unet_train(pl_unet u, int nsamples, int epochs, int batch, double lr, uns
     const double scale = 1.0 / (double(V0) * u->cused);
     for (int ep = 0; ep < epochs; ++ep) {
         std::shuffle(perm.begin(), perm.end(), rng);
+        // cosine decay of the learning rate from lr to lr / 20 over the epochs
+        const double ep_lr = lr * (0.05 + 0.95 * 0.5 * (1.0 + std::cos(3.14159265358979323846 * ep / std::max(1, epochs - 1))));
         UCK(cudaMemsetAsync(u->dacc, 0, sizeof(double), u->st));
         int nb = 0;
         for (int s0 = 0; s0 + batch <= nsamples; s0 += batch, ++nb) {
@@ -732,7 +734,7 @@ int pl_unet_train(pl_unet u, int nsamples, int epochs, int batch, double lr, uns
             pl::unet::k_mse<<<blocks_for((long long)batch * V0 * u->cout), 256, 0, u->st>>>(
                 u->pred, u->tgt, u->dpred, u->cout, u->cused, (long long)batch * V0, scale / batch, u->dacc);
             if ((r = backward(u, batch))) return r;
-            if ((r = adam(u, lr, 1.0f))) return r;
+            if ((r = adam(u, ep_lr, 1.0f))) return r;
         }
         double acc = 0;
         UCK(cudaMemcpyAsync(&acc, u->dacc, sizeof(double), cudaMemcpyDeviceToHost, u->st));

@@ -158,8 +158,13 @@ class ForcedParams:
         return side, inflow, outflow, adiabatic
 
     def program_ops(self, phase):
-        """Boundary calls of one time step in the order of test/nsadsens.cpp:81-103 (forward) and
-        :117-133 (adjoint)."""
+        """Boundary calls of one time step: those of test/nsadsens.cpp:81-103 (forward) and
+        :117-133 (adjoint), with both SmoothCorner calls moved to the end of the step as in
+        production/heatsink.cpp:155-168. The values are the same: the AD / AAD routines read and
+        write only g (and the previous collide's velocity), the f-set smoothing reads and writes
+        only f, and the outlet's adjoint pressure routine, which reads g, acts on no node the
+        smoothing writes (the outlet excludes the channel walls' edges). With every smoothing
+        call last, the device runs the program on its staged boundary path."""
         F = faces(self.nd, self.lx, self.ly, self.lz)
         side, inflow, outflow, adiabatic = self.masks()
         wall = side.astype(np.int32)
@@ -174,14 +179,13 @@ class ForcedParams:
                     for (a, p, d) in F]
             ops += [dict(kind=A.BC_NS_RHO, lat=0, axis=a, pos=p, dir=d, type=m_out, v0=one, v1=zero, v2=zero)
                     for (a, p, d) in F]
-            ops.append(dict(kind=A.SMOOTH_CORNER, lat=0))
             ops += [dict(kind=A.BC_AD_T, lat=1, axis=a, pos=p, dir=d, type=m_in, c0=0.0) for (a, p, d) in F]
             ops += [dict(kind=A.BC_AD_Q, lat=1, axis=a, pos=p, dir=d, type=m_q, c0=0.0) for (a, p, d) in F]
+            ops.append(dict(kind=A.SMOOTH_CORNER, lat=0))
             ops.append(dict(kind=A.SMOOTH_CORNER, lat=1))
         else:
             ops += [dict(kind=A.BC_AAD_T, lat=1, axis=a, pos=p, dir=d, type=m_in) for (a, p, d) in F]
             ops += [dict(kind=A.BC_AAD_Q, lat=1, axis=a, pos=p, dir=d, type=m_q) for (a, p, d) in F]
-            ops.append(dict(kind=A.SMOOTH_CORNER, lat=1))
             ops += [dict(kind=A.BC_IWALL, lat=0, axis=a, pos=p, dir=d, type=wall) for (a, p, d) in F]
             ops += [dict(kind=A.BC_ANS_U, lat=0, axis=a, pos=p, dir=d, type=m_in, v0=u, v1=zero, v2=zero)
                     for (a, p, d) in F]
@@ -189,6 +193,7 @@ class ForcedParams:
                 ops += [dict(kind=A.BC_AAD_RHO, lat=0, axis=a, pos=p, dir=d, type=2 * m_out) for (a, p, d) in F]
             else:
                 ops += [dict(kind=A.BC_ANS_RHO, lat=0, axis=a, pos=p, dir=d, type=m_out) for (a, p, d) in F]
+            ops.append(dict(kind=A.SMOOTH_CORNER, lat=1))
             ops.append(dict(kind=A.SMOOTH_CORNER, lat=0))
         return ops
 
@@ -205,11 +210,13 @@ class ForcedHeatSink:
     iteration (filter, forward and adjoint to the residual tolerance, sensitivity, filtered
     sensitivity) of production/heatsink.cpp:94-244 with this problem's physics."""
 
-    def __init__(self, p, storage="fp64"):
+    def __init__(self, p, storage="fp64", stochastic_rounding=False):
         self.p = p
         self.q = 9 if p.nd == 2 else 15
         self.n = p.n
         self.lp = LatticePair(self.q, p.lx, p.ly, p.lz, storage)
+        if stochastic_rounding:
+            self.lp.set_option(A.OPT_STOCHASTIC_ROUNDING, 1)
         self.prog_f = self.lp.program(to_descs(p.program_ops("forward")))
         self.prog_a = self.lp.program(to_descs(p.program_ops("adjoint")))
         self.ph = phys(nu=p.nu)

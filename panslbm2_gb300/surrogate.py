@@ -279,6 +279,8 @@ def main(argv=None):
     ap.add_argument("--out", required=True)
     ap.add_argument("--log", default=None)
     ap.add_argument("--eval-seed", type=int, default=0)
+    ap.add_argument("--max-adjoint-steps", type=int, default=25000,
+                    help="training designs whose adjoint does not converge within this are skipped")
     a = ap.parse_args(argv)
     nx, ny, nz = (int(v) for v in a.shape.split(","))
     p = ForcedParams(3, nx, ny, nz)
@@ -292,6 +294,7 @@ def main(argv=None):
 
     t0 = time.perf_counter()
     rec["samples"] = sw.generate(a.nsamples, a.first_seed, tol=a.data_tol or a.tol,
+                                 max_adjoint_steps=a.max_adjoint_steps,
                                  log=lambda d: (log.append(d), out(dict(sample=d))))
     rec["generate_s"] = round(time.perf_counter() - t0, 2)
     used = [d["seed"] for d in rec["samples"] if d["used"]]

@@ -15,8 +15,9 @@ from panslbm2_gb300.design import HeatSinkDesign
 pytestmark = pytest.mark.gpu
 
 
-def test_adjoint_sensitivity_matches_finite_differences():
-    p = HS.Params(2, 40, 30)
+@pytest.mark.parametrize("L", [4.0, 8.0])
+def test_adjoint_sensitivity_matches_finite_differences(L):
+    p = HS.Params(2, 40, 30, L=L)
     s = np.clip(HS.grf_design(2, 40, 30, seed=1, sigma=4.0), 0.05, 0.95)
     hs = HeatSinkDesign(p, "fp64")
     # 400k steps: the adjoint converges to 1e-9; the forward velocity residual of this design
