@@ -401,6 +401,75 @@ def precision_leg(nf=4000, na=4000):
     return out
 
 
+def dropin_leg(steps=400):
+    """The drop-in: a heat-sink driver written against the reference's template API
+    (tests/dropin/heatsink_driver.cpp, the calls of production/heatsink3D.cpp's forward loop in
+    the same order, saving every step) built on dropin/src, on the 160x160x80 lattice with FP32
+    storage; its loop time against pl_step's on the same workload"""
+    import shutil
+    import struct
+    import tempfile
+    from panslbm2_gb300 import heatsink as HS
+    cxx = shutil.which("g++")
+    if cxx is None:
+        return {"error": "g++ not found"}
+    tmp = tempfile.mkdtemp(prefix="dropin_")
+    exe = os.path.join(tmp, "heatsink_driver")
+    lib = os.path.join(ROOT, "panslbm2_gb300")
+    subprocess.check_call([cxx, "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"),
+                           os.path.join(ROOT, "tests", "dropin", "heatsink_driver.cpp"), "-L", lib, "-lpanslbm_gb300",
+                           "-Wl,-rpath," + lib, "-o", exe])
+    p = HS.Params(3, 160, 160, 80)
+    n = p.lx * p.ly * p.lz
+    ss = HS.grf_design(3, 160, 160, 80, seed=0, sigma=8.0)
+    alpha, kappa, dads, dkds = p.design_fields(ss)
+    zero, one = np.zeros(n), np.ones(n)
+    fields = [alpha, kappa, dads, dkds, one, zero, zero, zero, zero] + [zero] * 8
+    fin, fout = os.path.join(tmp, "in.bin"), os.path.join(tmp, "out.bin")
+    res = {}
+    for nsteps in (20, steps):
+        with open(fin, "wb") as fh:
+            fh.write(struct.pack("6i", 3, p.lx, p.ly, p.lz, nsteps, 1))
+            fh.write(struct.pack("7d", p.nu, p.gx, p.gy, p.gz, p.tem0, p.qn, p.L))
+            for v in fields:
+                fh.write(np.ascontiguousarray(v, np.float64).tobytes())
+        env = dict(os.environ, PANSLBM2_GPU_STORAGE="fp32")
+        r = subprocess.run([exe, "fwd", fin, fout], capture_output=True, text=True, env=env, check=True)
+        for line in r.stderr.splitlines():
+            if line.startswith("loop_seconds"):
+                res[nsteps] = float(line.split()[1])
+    shutil.rmtree(tmp, ignore_errors=True)
+    # the per-step rate from the difference of a long and a short run (start-up excluded)
+    per_step = (res[steps] - res[20]) / (steps - 20)
+    # pl_step on the same workload with the same every-step saves, for the ratio
+    from panslbm2_gb300 import _capi as A
+    from panslbm2_gb300.lattice import LatticePair, phys
+    S = Setup(WORKLOADS["heatsink3d-160x160x80-fp32"])
+    lp = LatticePair(S.q, S.lx, S.ly, S.lz, S.storage)
+    for fid, v in S.fields.items():
+        lp.set_field(fid, v)
+    lp.init(0, one, ux=zero, uy=zero, uz=zero)
+    lp.init(1, zero, ux=zero, uy=zero, uz=zero)
+    prog = lp.program(HS.to_descs(S.ops))
+    ph = phys(**S.phys)
+    lp.collide(S.kind, ph)
+    for _ in range(20):
+        lp.step(S.kind, ph, prog, save=True)
+    lp.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        lp.step(S.kind, ph, prog, save=True)
+    lp.synchronize()
+    api = (time.perf_counter() - t0) / steps
+    lp.close()
+    return {"lattice": "heatsink3d-160x160x80-fp32 (storage fp32, host arrays float64)", "steps": steps,
+            "loop_seconds": round(res[steps], 4), "ms_per_step": round(per_step * 1e3, 4),
+            "mlups": round(n / per_step / 1e6, 1), "pl_step_saving_ms": round(api * 1e3, 4),
+            "ratio_to_pl_step": round(per_step / api, 3),
+            "what": "forward loop of a driver on the template API, collide with saves every step + 2 streams + "
+                    "boundary calls + smoothing, outputs left on the device until the next phase boundary"}
+
+
 def fp64_leg(steps=200):
     """FP64 step on the 1600x800 forced heat sink against both of its ceilings: HBM (312
     algorithmic bytes per node) and the FP64 FMA rate probed on this device; the FP64 operations
@@ -607,6 +676,7 @@ def main():
         leg(line, "design_iter_3d_surrogate", surrogate_leg)
         leg(line, "precision_errors", precision_leg)
         leg(line, "fp64_roofline", fp64_leg)
+        leg(line, "dropin", dropin_leg)
     if rank == 0 and not args.no_transient:
         leg(line, "transient_iter", transient_gpu)
     if rank == 0 and not args.no_cpu:

@@ -94,6 +94,7 @@ namespace PANSLBM2 {
         void InitialCondition(Q<T>& _q, const T *_ux, const T *_uy, const T *_item, const T *_iqx, const T *_iqy) {
             gpu::Pair &pr = gpu::own(_q, 1);
             pr.flush();
+            gpu::sync_outputs();
             gpu::AsDouble<T> x(_ux, pr.n), y(_uy, pr.n), it(_item, pr.n), qx(_iqx, pr.n), qy(_iqy, pr.n);
             std::vector<double> z(pr.n, 0.0);
             gpu::ck(pl_init(pr.h, 3, it.p, qx.p, qy.p, z.data(), x.p, y.p, z.data()), "pl_init");
@@ -102,6 +103,7 @@ namespace PANSLBM2 {
         void InitialCondition(Q<T>& _q, const T *_ux, const T *_uy, const T *_uz, const T *_item, const T *_iqx, const T *_iqy, const T *_iqz) {
             gpu::Pair &pr = gpu::own(_q, 1);
             pr.flush();
+            gpu::sync_outputs();
             gpu::AsDouble<T> x(_ux, pr.n), y(_uy, pr.n), z(_uz, pr.n), it(_item, pr.n), qx(_iqx, pr.n), qy(_iqy, pr.n), qz(_iqz, pr.n);
             gpu::ck(pl_init(pr.h, 3, it.p, qx.p, qy.p, qz.p, x.p, y.p, z.p), "pl_init");
         }

@@ -20,6 +20,7 @@ namespace PANSLBM2 {
         void InitialCondition(P<T>& _p, const T *_irho, const T *_imx, const T *_imy, const T *_isxx, const T *_isxy, const T *_isyx, const T *_isyy, const T *_gamma) {
             gpu::Pair &pr = gpu::own(_p, 0);
             pr.flush();
+            gpu::sync_outputs();
             pr.input(PL_GAMMA, _gamma);
             gpu::AsDouble<T> r(_irho, pr.n), x(_imx, pr.n), y(_imy, pr.n), a(_isxx, pr.n), b(_isxy, pr.n), c(_isyx, pr.n), d(_isyy, pr.n);
             const double *in[7] = {r.p, x.p, y.p, a.p, b.p, c.p, d.p};
@@ -51,6 +52,7 @@ namespace PANSLBM2 {
         void SensitivityCompliance(P<T>& _p, T *_dfds, const T *_sxx, const T *_sxy, const T *_syx, const T *_syy, const T *_irho, const T *_isxx, const T *_isxy, const T *_isyx, const T *_isyy) {
             gpu::Pair &pr = gpu::own(_p, 0);
             pr.flush();
+            gpu::sync_outputs();
             gpu::AsDouble<T> a(_sxx, pr.n), b(_sxy, pr.n), c(_syx, pr.n), d(_syy, pr.n), r(_irho, pr.n), e(_isxx, pr.n),
                 f(_isxy, pr.n), g(_isyx, pr.n), h(_isyy, pr.n);
             const double *in[9] = {a.p, b.p, c.p, d.p, r.p, e.p, f.p, g.p, h.p};

@@ -34,6 +34,7 @@ namespace PANSLBM2 {
         void InitialCondition(P<T>& _p, const T *_ux, const T *_uy, const T *_ip, const T *_iux, const T *_iuy) {
             gpu::Pair &pr = gpu::own(_p, 0);
             pr.flush();
+            gpu::sync_outputs();
             gpu::AsDouble<T> x(_ux, pr.n), y(_uy, pr.n), ip(_ip, pr.n), ix(_iux, pr.n), iy(_iuy, pr.n);
             std::vector<double> z(pr.n, 0.0);
             gpu::ck(pl_init(pr.h, 2, ip.p, ix.p, iy.p, z.data(), x.p, y.p, z.data()), "pl_init");
@@ -42,6 +43,7 @@ namespace PANSLBM2 {
         void InitialCondition(P<T>& _p, const T *_ux, const T *_uy, const T *_uz, const T *_ip, const T *_iux, const T *_iuy, const T *_iuz) {
             gpu::Pair &pr = gpu::own(_p, 0);
             pr.flush();
+            gpu::sync_outputs();
             gpu::AsDouble<T> x(_ux, pr.n), y(_uy, pr.n), z(_uz, pr.n), ip(_ip, pr.n), ix(_iux, pr.n), iy(_iuy, pr.n), iz(_iuz, pr.n);
             gpu::ck(pl_init(pr.h, 2, ip.p, ix.p, iy.p, iz.p, x.p, y.p, z.p), "pl_init");
         }

@@ -30,6 +30,7 @@ namespace PANSLBM2 {
             (void)_ux; (void)_uy;
             gpu::Pair &pr = gpu::own(_p, 0);
             pr.flush();
+            gpu::sync_outputs();
             gpu::AsDouble<T> ip(_ip, pr.n), ix(_iux, pr.n), iy(_iuy, pr.n);
             gpu::ck(pl_init(pr.h, 5, ip.p, ix.p, iy.p, nullptr, nullptr, nullptr, nullptr), "pl_init");
         }

@@ -86,6 +86,7 @@ namespace PANSLBM2 {
         void InitialCondition(Q<T>& _q, const T *_tem, const T *_ux, const T *_uy) {
             gpu::Pair &pr = gpu::own(_q, 1);
             pr.flush();
+            gpu::sync_outputs();
             gpu::AsDouble<T> t(_tem, pr.n), x(_ux, pr.n), y(_uy, pr.n);
             std::vector<double> z(pr.n, 0.0);
             gpu::ck(pl_init(pr.h, 1, t.p, nullptr, nullptr, nullptr, x.p, y.p, z.data()), "pl_init");
@@ -94,6 +95,7 @@ namespace PANSLBM2 {
         void InitialCondition(Q<T>& _q, const T *_tem, const T *_ux, const T *_uy, const T *_uz) {
             gpu::Pair &pr = gpu::own(_q, 1);
             pr.flush();
+            gpu::sync_outputs();
             gpu::AsDouble<T> t(_tem, pr.n), x(_ux, pr.n), y(_uy, pr.n), z(_uz, pr.n);
             gpu::ck(pl_init(pr.h, 1, t.p, nullptr, nullptr, nullptr, x.p, y.p, z.p), "pl_init");
         }

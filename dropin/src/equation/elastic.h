@@ -30,6 +30,7 @@ namespace PANSLBM2 {
         void InitialCondition(P<T>& _p, const T *_rho, const T *_ux, const T *_uy, const T *_sxx, const T *_sxy, const T *_syx, const T *_syy) {
             gpu::Pair &pr = gpu::own(_p, 0);
             pr.flush();
+            gpu::sync_outputs();
             gpu::AsDouble<T> r(_rho, pr.n), x(_ux, pr.n), y(_uy, pr.n), a(_sxx, pr.n), b(_sxy, pr.n), c(_syx, pr.n), d(_syy, pr.n);
             const double *in[7] = {r.p, x.p, y.p, a.p, b.p, c.p, d.p};
             gpu::ck(pl_init_elastic(pr.h, 0, in), "pl_init_elastic");

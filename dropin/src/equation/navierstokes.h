@@ -41,6 +41,7 @@ namespace PANSLBM2 {
         void InitialCondition(P<T>& _p, const T *_rho, const T *_ux, const T *_uy) {
             gpu::Pair &pr = gpu::own(_p, 0);
             pr.flush();
+            gpu::sync_outputs();
             gpu::AsDouble<T> r(_rho, pr.n), x(_ux, pr.n), y(_uy, pr.n);
             std::vector<double> z(pr.n, 0.0);
             gpu::ck(pl_init(pr.h, 0, r.p, nullptr, nullptr, nullptr, x.p, y.p, z.data()), "pl_init");
@@ -49,6 +50,7 @@ namespace PANSLBM2 {
         void InitialCondition(P<T>& _p, const T *_rho, const T *_ux, const T *_uy, const T *_uz) {
             gpu::Pair &pr = gpu::own(_p, 0);
             pr.flush();
+            gpu::sync_outputs();
             gpu::AsDouble<T> r(_rho, pr.n), x(_ux, pr.n), y(_uy, pr.n), z(_uz, pr.n);
             gpu::ck(pl_init(pr.h, 0, r.p, nullptr, nullptr, nullptr, x.p, y.p, z.p), "pl_init");
         }

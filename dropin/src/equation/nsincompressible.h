@@ -28,6 +28,7 @@ namespace PANSLBM2 {
         void InitialCondition(P<T>& _p, const T *_rho, const T *_ux, const T *_uy) {
             gpu::Pair &pr = gpu::own(_p, 0);
             pr.flush();
+            gpu::sync_outputs();
             gpu::AsDouble<T> r(_rho, pr.n), x(_ux, pr.n), y(_uy, pr.n);
             gpu::ck(pl_init(pr.h, 4, r.p, nullptr, nullptr, nullptr, x.p, y.p, nullptr), "pl_init");
         }

@@ -43,6 +43,7 @@
 #include <vector>
 
 #include "panslbm_gb300.h"
+#include "../utility/vtkio.h"
 
 namespace PANSLBM2 {
 namespace {
@@ -250,6 +251,7 @@ inline void finish_rec(BcRec &r, int sets, int inputs, double eps = 0.0, double 
 struct Shadow {
     const void *ptr = nullptr;
     std::vector<double> copy;
+    long long epoch = -1;   // the phase it was last compared in
 };
 
 struct Pair;
@@ -258,6 +260,31 @@ inline std::map<const void *, Pair *> &saved_arrays() {
     static std::map<const void *, Pair *> m;
     return m;
 }
+
+//  Host output arrays whose values are still on the device: a saving collide leaves its outputs in
+//  the library's two save slots per family and records here which save each host array stands
+//  for. They are written back when the driver reaches a phase boundary (an initial condition, a
+//  sensitivity, a filter, an export, a population copy: sync_outputs) or just before their save
+//  slot is overwritten (two saves later, when the array is not saved into again). Inside a time
+//  loop nothing is copied to the host: the residual reads the device slots.
+struct Pending {
+    const void *key;  // the host array
+    Pair *pair;
+    bool adjoint;
+    int m;            // index in the family's outputs (rho ux uy uz tem qx qy qz / ip .. iqz)
+    long long gen;    // the family's save generation
+    bool is_float;
+};
+inline std::map<const void *, Pending> &pending_outputs() {
+    static std::map<const void *, Pending> m;
+    return m;
+}
+//  phases seen so far: host inputs are compared with their last upload once per phase
+inline long long &input_epoch() {
+    static long long e = 0;
+    return e;
+}
+inline void sync_outputs();
 inline std::vector<Pair *> &live_pairs() {
     static std::vector<Pair *> v;
     return v;
@@ -281,6 +308,7 @@ struct Pair {
     const void *fwd_save[8] = {}, *fwd_prev[8] = {};
     const void *adj_save[11] = {}, *adj_prev[11] = {};
     bool fwd_saved = false, adj_saved = false;
+    long long fwd_gen = 0, adj_gen = 0;   // saves per family
 
     // snapshots: the host array the device slot stands for, and whether the device copy still
     // has to be taken from the last collide
@@ -299,7 +327,28 @@ struct Pair {
             if (it->second == this) it = sa.erase(it);
             else ++it;
         }
+        write_back([](const Pending &) { return true; });
         if (h) pl_destroy(h);
+    }
+
+    //  copy the pending host outputs of this pair that `pick` selects from the device
+    template <class Pick>
+    void write_back(Pick pick) {
+        auto &po = pending_outputs();
+        std::vector<double> tmp;
+        for (auto it = po.begin(); it != po.end();) {
+            const Pending &e = it->second;
+            if (e.pair != this || !pick(e)) { ++it; continue; }
+            const long long age = (e.adjoint ? adj_gen : fwd_gen) - e.gen;
+            if (h && age <= 1) {
+                tmp.resize(n);
+                ck(pl_get_saved_field(h, (e.adjoint ? PL_IP : PL_RHO) + e.m, int(age), tmp.data()),
+                   "pl_get_saved_field");
+                if (e.is_float) to_host(static_cast<float *>(const_cast<void *>(it->first)), tmp);
+                else std::memcpy(const_cast<void *>(it->first), tmp.data(), sizeof(double) * n);
+            }
+            it = po.erase(it);
+        }
     }
 
     //  upload a host input when it is new or changed (PANSLBM2_GPU_TRUST_INPUTS=1: when new)
@@ -309,6 +358,9 @@ struct Pair {
         Shadow &s = shadows[field];
         static const bool trust = env_flag("PANSLBM2_GPU_TRUST_INPUTS");
         if (trust && s.ptr == p && s.copy.size() == (size_t)n) return;
+        // within one phase (between two phase-boundary calls) a known input is not compared again
+        if (s.ptr == p && s.copy.size() == (size_t)n && s.epoch == input_epoch()) return;
+        s.epoch = input_epoch();
         if (s.ptr == p && s.copy.size() == (size_t)n) {
             bool equal;
             if (std::is_same<T, double>::value) equal = std::memcmp(s.copy.data(), p, sizeof(double) * n) == 0;
@@ -471,6 +523,16 @@ struct Pair {
                              kind == PL_EL_COLLIDE || kind == PL_EL_EXTENDED || kind == PL_AEL_COLLIDE);
         const int slot = adjoint ? 1 : 0;
         const bool saves_snap = save && snap != nullptr;
+        if (save) {
+            // the save about to be written reuses the slot of the save before last: host arrays
+            // that still stand for that save, and are not saved into again now, take it first
+            const long long gen = adjoint ? adj_gen : fwd_gen;
+            write_back([&](const Pending &e) {
+                if (e.adjoint != adjoint || gen - e.gen < 1) return false;
+                for (int m = 0; m < nouts; ++m) if (outs[m] && (const void *)outs[m] == e.key) return false;
+                return true;
+            });
+        }
         std::vector<int> idx;
         if (!queue.empty() && fusable(adjoint, has_g, idx)) {
             settle_snapshot(0, adjoint ? nullptr : snap, !adjoint && saves_snap);
@@ -486,15 +548,14 @@ struct Pair {
             ck(pl_collide(h, kind, &ph, save ? 1 : 0), "pl_collide");
         }
         if (save) {
-            const int base = adjoint ? PL_IP : PL_RHO;
-            std::vector<double> tmp(n);
             const void **cur = adjoint ? adj_save : fwd_save, **prev = adjoint ? adj_prev : fwd_prev;
+            const long long gen = ++(adjoint ? adj_gen : fwd_gen);
             for (int m = 0; m < nouts; ++m) {
                 prev[m] = cur[m];
                 cur[m] = outs[m];
                 if (!outs[m]) continue;
-                ck(pl_get_field(h, base + m, tmp.data()), "pl_get_field");
-                to_host(outs[m], tmp);
+                // the values stay on the device until the host needs them (sync_outputs)
+                pending_outputs()[outs[m]] = Pending{outs[m], this, adjoint, m, gen, !std::is_same<T, double>::value};
                 saved_arrays()[outs[m]] = this;
             }
             (adjoint ? adj_saved : fwd_saved) = true;
@@ -528,6 +589,15 @@ struct Pair {
         return -1;
     }
 };
+
+//  phase boundary: every host output array takes its value from the device, and host inputs are
+//  compared with their uploads again at their next use
+inline void sync_outputs() {
+    for (Pair *p : live_pairs()) p->write_back([](const Pending &) { return true; });
+    ++input_epoch();
+}
+//  the VTK exporters read host arrays through the driver's functors: sync before they do
+inline const bool vtk_hook_set = (vtkio::host_sync_hook() = &sync_outputs, true);
 
 //  Base of the drop-in particles: the handle binding and the particle's role (0 NS set, 1 AD
 //  set, -1 not known yet).
@@ -650,6 +720,7 @@ void sensitivity(Pair &pr, int which, T *dfds, const T *dads, const T *dkds, con
                  const T *iqz, const T *kappa, const T *g, const T *ig, const double *qn, const int *mask) {
     pr.flush();
     pr.settle_all();
+    sync_outputs();
     pr.input(PL_FWD_UX, ux);
     pr.input(PL_FWD_UY, uy);
     pr.input(PL_FWD_UZ, uz);

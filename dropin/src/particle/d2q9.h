@@ -87,6 +87,7 @@ public:
         void CopyToHost() {
             gpu::Pair &pr = *this->gpu.pair;
             pr.flush();
+            gpu::sync_outputs();
             std::vector<double> p((size_t)nc*this->nxyz);
             gpu::ck(pl_get_populations(pr.h, this->gpu.set, p.data()), "pl_get_populations");
             for (int idx = 0; idx < this->nxyz; ++idx) {
@@ -97,6 +98,7 @@ public:
         void CopyFromHost() {
             gpu::Pair &pr = *this->gpu.pair;
             pr.flush();
+            gpu::sync_outputs();
             std::vector<double> p((size_t)nc*this->nxyz);
             for (int idx = 0; idx < this->nxyz; ++idx) {
                 p[idx] = double(this->f0[idx]);

@@ -10,6 +10,7 @@ namespace PANSLBM2 {
         template<class T, template<class>class P, class F>
         std::vector<T> GetFilteredValue(P<T>& _p, T _R, const std::vector<T> &_v, F _weight) {
             gpu::Pair &pr = *_p.gpu_particle().pair;
+            gpu::sync_outputs();
             const std::vector<int> &mask = gpu::filter_mask(pr, double(_R), _weight);
             std::vector<double> v(_v.begin(), _v.end()), out(pr.n);
             gpu::ck(pl_density_filter(pr.h, double(_R), v.data(), mask.empty() ? nullptr : mask.data(), out.data()),
@@ -20,6 +21,7 @@ namespace PANSLBM2 {
         template<class T, template<class>class P>
         std::vector<T> GetFilteredValue(P<T>& _p, T _R, const std::vector<T> &_v) {
             gpu::Pair &pr = *_p.gpu_particle().pair;
+            gpu::sync_outputs();
             std::vector<double> v(_v.begin(), _v.end()), out(pr.n);
             gpu::ck(pl_density_filter(pr.h, double(_R), v.data(), nullptr, out.data()), "pl_density_filter");
             return std::vector<T>(out.begin(), out.end());

@@ -14,6 +14,7 @@ namespace PANSLBM2 {
         template<class T, template<class>class P, class F>
         std::vector<T> GetFilteredVariable(P<T>& _p, T _R, T _beta, const std::vector<T> &_s, F _weight) {
             gpu::Pair &pr = *_p.gpu_particle().pair;
+            gpu::sync_outputs();
             const std::vector<int> &mask = gpu::filter_mask(pr, double(_R), _weight);
             std::vector<double> s(_s.begin(), _s.end()), out(pr.n);
             gpu::ck(pl_heaviside_var(pr.h, double(_R), double(_beta), s.data(), mask.empty() ? nullptr : mask.data(), out.data()),
@@ -24,6 +25,7 @@ namespace PANSLBM2 {
         template<class T, template<class>class P>
         std::vector<T> GetFilteredVariable(P<T>& _p, T _R, T _beta, const std::vector<T> &_s) {
             gpu::Pair &pr = *_p.gpu_particle().pair;
+            gpu::sync_outputs();
             std::vector<double> s(_s.begin(), _s.end()), out(pr.n);
             gpu::ck(pl_heaviside_var(pr.h, double(_R), double(_beta), s.data(), nullptr, out.data()), "pl_heaviside_var");
             return std::vector<T>(out.begin(), out.end());
@@ -32,6 +34,7 @@ namespace PANSLBM2 {
         template<class T, template<class>class P, class F>
         std::vector<T> GetFilteredSensitivity(P<T>& _p, T _R, T _beta, const std::vector<T> &_s, const std::vector<T> &_dfdrho, F _weight) {
             gpu::Pair &pr = *_p.gpu_particle().pair;
+            gpu::sync_outputs();
             const std::vector<int> &mask = gpu::filter_mask(pr, double(_R), _weight);
             std::vector<double> s(_s.begin(), _s.end()), d(_dfdrho.begin(), _dfdrho.end()), out(pr.n);
             gpu::ck(pl_heaviside_sens(pr.h, double(_R), double(_beta), s.data(), d.data(), mask.empty() ? nullptr : mask.data(),
@@ -42,6 +45,7 @@ namespace PANSLBM2 {
         template<class T, template<class>class P>
         std::vector<T> GetFilteredSensitivity(P<T>& _p, T _R, T _beta, const std::vector<T> &_s, const std::vector<T> &_dfdrho) {
             gpu::Pair &pr = *_p.gpu_particle().pair;
+            gpu::sync_outputs();
             std::vector<double> s(_s.begin(), _s.end()), d(_dfdrho.begin(), _dfdrho.end()), out(pr.n);
             gpu::ck(pl_heaviside_sens(pr.h, double(_R), double(_beta), s.data(), d.data(), nullptr, out.data()), "pl_heaviside_sens");
             return std::vector<T>(out.begin(), out.end());

@@ -64,6 +64,7 @@ public:
             std::vector<double> dg((size_t)this->m * this->n);
             for (int i = 0; i < this->m; ++i)
                 for (int j = 0; j < this->n; ++j) dg[(size_t)i * this->n + j] = double(_dgdx[i][j]);
+            gpu::sync_outputs();
             gpu::ck(pl_mma_update(this->h, x.data(), double(_f), df.data(), g.data(), dg.data()), "pl_mma_update");
             for (int j = 0; j < this->n; ++j) _xk[j] = T(x[j]);
             this->previousvalue = _f;

@@ -64,6 +64,7 @@ private:
         //  the functors' values at every node in (k, j, i) order, taken on the calling thread
         template<class... Fs>
         std::shared_ptr<std::vector<vtkio::Val>> take(Fs... _f) {
+            vtkio::host_sync();
             constexpr int cmp = sizeof...(Fs);
             auto v = std::make_shared<std::vector<vtkio::Val>>((size_t)this->nx * this->ny * this->nz * cmp);
             size_t o = 0;

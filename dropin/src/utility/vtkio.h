@@ -30,6 +30,16 @@
 namespace PANSLBM2 {
 namespace vtkio {
 
+//  Set by the device runtime (gpu/runtime.h): brings the host arrays that saving collides left on
+//  the device up to date before an exporter's functors read them. Unset for host-only use.
+inline void (*&host_sync_hook())() {
+    static void (*h)() = nullptr;
+    return h;
+}
+inline void host_sync() {
+    if (host_sync_hook()) host_sync_hook()();
+}
+
 //  one value as a default-formatted std::ostream prints it
 struct Val {
     double d;

@@ -62,6 +62,7 @@ public:
         void AddPointData(P<T>& _p, std::string _label, Fs ..._values) {
             constexpr int cmp = sizeof...(Fs);
             static_assert(cmp == 1 || cmp == 3 || cmp == 9, "AddPointData takes 1, 3 or 9 functors");
+            vtkio::host_sync();
             const int nnx = _p.nx + (_p.PEx != _p.mx - 1 ? 1 : 0), nny = _p.ny + (_p.PEy != _p.my - 1 ? 1 : 0);
             const int nnz = _p.nz + (_p.PEz != _p.mz - 1 ? 1 : 0);
             auto v = std::make_shared<std::vector<double>>((size_t)nnx * nny * nnz * cmp);

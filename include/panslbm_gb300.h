@@ -203,6 +203,11 @@ int pl_get_populations(pl_lattice h, int set, double *host);
 /* node fields */
 int pl_set_field(pl_lattice h, int field, const double *host);
 int pl_get_field(pl_lattice h, int field, double *host);
+/* a macroscopic field (PL_RHO..PL_QZ, PL_IP..PL_IQZ) of the last (age 0) or the previous (age 1)
+ * saving collide of its family; the device keeps both (the residual compares them), so a caller
+ * that mirrors host arrays can leave outputs on the device until it needs them (no counterpart in
+ * the reference, whose routines write host arrays directly) */
+int pl_get_saved_field(pl_lattice h, int field, int age, double *host);
 /* copy the forward macros of the last saving collide into PL_FWD_* */
 int pl_freeze_forward(pl_lattice h);
 

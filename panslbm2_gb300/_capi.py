@@ -58,7 +58,7 @@ class BcDesc(C.Structure):
 EXPORTS = [
     "pl_create", "pl_destroy", "pl_last_error", "pl_synchronize", "pl_set_stream", "pl_set_option",
     "pl_set_shift", "pl_set_inflow_scale",
-    "pl_set_populations", "pl_get_populations", "pl_set_field", "pl_get_field", "pl_freeze_forward",
+    "pl_set_populations", "pl_get_populations", "pl_set_field", "pl_get_field", "pl_get_saved_field", "pl_freeze_forward",
     "pl_program_create", "pl_program_destroy", "pl_init", "pl_init_elastic", "pl_collide", "pl_step", "pl_steps", "pl_stream",
     "pl_solve", "pl_snapshot", "pl_set_snapshot", "pl_residual", "pl_residual_host", "pl_residual_device_noalloc",
     "pl_sensitivity", "pl_sensitivity_compliance", "pl_store", "pl_load", "pl_store_release", "pl_store_swap_snapshot",

@@ -1061,6 +1061,23 @@ int pl_get_field(pl_lattice h, int f, double *host) {
     return download(h, host, src, h->n);
 }
 
+int pl_get_saved_field(pl_lattice h, int f, int age, double *host) {
+    PL_RANGE("pl_get_saved_field");
+    if (!h || !host || (age != 0 && age != 1)) return fail(PL_ERR_ARG, "bad arguments");
+    const double *src = nullptr;
+    if (f >= PL_RHO && f <= PL_QZ) {
+        const int s = age == 0 ? h->fwd_saved : h->fwd_prev_saved;
+        src = s >= 0 ? h->fwd[s][f - PL_RHO] : nullptr;
+    } else if (f >= PL_IP && f <= PL_IQZ) {
+        const int s = age == 0 ? h->adj_saved : h->adj_prev_saved;
+        src = s >= 0 ? h->adj[s][f - PL_IP] : nullptr;
+    } else {
+        return fail(PL_ERR_ARG, "field %d is not a saved macroscopic field", f);
+    }
+    if (!src) return fail(PL_ERR_STATE, "no save of age %d holds field %d", age, f);
+    return download(h, host, src, h->n);
+}
+
 int pl_freeze_forward(pl_lattice h) {
     if (!h) return fail(PL_ERR_ARG, "null handle");
     if (h->fwd_saved < 0) return fail(PL_ERR_STATE, "no saved forward collide");

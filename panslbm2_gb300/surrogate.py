@@ -256,6 +256,29 @@ def default_weights_path():
     return os.path.join(os.path.dirname(os.path.abspath(__file__)), "weights", "unet3d_forced_160x160x80.npz")
 
 
+def profile_main(argv):
+    """python -m panslbm2_gb300.surrogate profile [--shape X,Y,Z] [--iters K]: K forward + backward
+    + Adam passes of the U-Net on random inputs (a fixed kernel sequence for ncu captures)"""
+    import argparse
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--shape", default="160,160,80")
+    ap.add_argument("--iters", type=int, default=3)
+    ap.add_argument("--levels", type=int, default=4)
+    ap.add_argument("--base", type=int, default=16)
+    a = ap.parse_args(argv)
+    nx, ny, nz = (int(v) for v in a.shape.split(","))
+    net = UNet(nx, ny, nz, a.levels, a.base, 1)
+    rng = np.random.default_rng(0)
+    net.reserve(1, len(TARGETS))
+    net.set_static(rng.random((nx * ny * nz, 7)).astype(np.float32))
+    net.add_sample(0, rng.random(nx * ny * nz), 0.01 * rng.standard_normal((len(TARGETS), nx * ny * nz)))
+    t0 = time.perf_counter()
+    loss = net.train(1, a.iters, 1, 1e-3, seed=0)
+    print(json.dumps(dict(shape=[nx, ny, nz], iters=a.iters, seconds=round(time.perf_counter() - t0, 4),
+                          loss=[float(v) for v in loss])))
+    net.close()
+
+
 def main(argv=None):
     """python -m panslbm2_gb300.surrogate --nsamples N --epochs E --out weights.npz [--log log.json]
 
@@ -325,4 +348,8 @@ def main(argv=None):
 
 
 if __name__ == "__main__":
-    main()
+    import sys
+    if len(sys.argv) > 1 and sys.argv[1] == "profile":
+        profile_main(sys.argv[2:])
+    else:
+        main()

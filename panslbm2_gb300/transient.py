@@ -183,3 +183,40 @@ class TransientHeatSink:
         else:
             objective = float(np.sum(acc[self.mask != 0])) / (self.p.L * nt)
         return dict(objective=objective, dfdss=dfdss, times=times, segments=nseg)
+
+
+def main(argv=None):
+    """python -m panslbm2_gb300.transient [--shape X,Y,Z] [--levels N] [--every K] [--physics forced|natural]:
+    one timed transient evaluation (after a short warm-up), FP32, seeded design 0"""
+    import argparse
+    import json
+    from . import forced as FC
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--shape", default="96,96,48")
+    ap.add_argument("--levels", type=int, default=202)
+    ap.add_argument("--every", type=int, default=100)
+    ap.add_argument("--physics", default="forced", choices=["forced", "natural"])
+    ap.add_argument("--storage", default="fp32")
+    a = ap.parse_args(argv)
+    nx, ny, nz = (int(v) for v in a.shape.split(","))
+    if a.physics == "forced":
+        p = FC.ForcedParams(3, nx, ny, nz)
+        ss = p.project(p.design(seed=0))
+        tr = TransientHeatSink(p, a.storage, checkpoint_every=a.every)
+        run = lambda nt: tr.evaluate_design(ss, nt)  # noqa: E731
+    else:
+        p = HS.Params(3, nx, ny, nz)
+        ss = HS.grf_design(3, nx, ny, nz, seed=0, sigma=8.0)
+        alpha, kappa, dads, dkds = p.design_fields(ss)
+        tr = TransientHeatSink(p, a.storage, checkpoint_every=a.every)
+        run = lambda nt: tr.evaluate(alpha, kappa, dads, dkds, nt)  # noqa: E731
+    run(min(a.levels, 2 * a.every + 2))
+    t0 = time.perf_counter()
+    r = run(a.levels)
+    print(json.dumps(dict(shape=[nx, ny, nz], levels=a.levels, every=a.every, physics=a.physics,
+                          seconds=round(time.perf_counter() - t0, 4), phases=r["times"], objective=r["objective"])))
+    tr.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -10,6 +10,7 @@
 //          it0 iqx0 iqy0 iqz0
 //  output: fwd: f (q*N, direction-major), g, rho ux uy uz tem qx qy qz
 //          adj: f, g, ip iux iuy iuz imx imy imz item iqx iqy iqz, sens0..sens3
+#include <chrono>
 #include <cstdio>
 #include <cstdlib>
 #include <string>
@@ -152,6 +153,7 @@ int run3d(const Input &in, bool adj, FILE *out) {
     AD::InitialCondition(pg, A[8].data(), A[5].data(), A[6].data(), A[7].data());
     double *pux = ux.data(), *puy = uy.data(), *puz = uz.data(), *puxp = uxp.data(), *puyp = uyp.data(), *puzp = uzp.data();
     double *pqx = qx.data(), *pqy = qy.data(), *pqz = qz.data(), *pqxp = qxp.data(), *pqyp = qyp.data(), *pqzp = qzp.data();
+    const auto t0 = std::chrono::steady_clock::now();
     for (int t = 1; t <= in.tf; ++t) {
         AD::MacroBrinkmanCollideNaturalConvection(pf, rho.data(), pux, puy, puz, A[0].data(), in.nu, pg, tem.data(), pqx, pqy,
                                                   pqz, A[1].data(), in.gx, in.gy, in.gz, tem0, true, gi.data());
@@ -170,7 +172,11 @@ int run3d(const Input &in, bool adj, FILE *out) {
         std::swap(pqx, pqxp); std::swap(pqy, pqyp); std::swap(pqz, pqzp);
     }
     if (!adj) {
-        put(out, populations(pf).data(), (size_t)15 * n);
+        // the time loop's wall time (its outputs written back by the next call, CopyToHost below)
+        const auto pop = populations(pf);
+        std::fprintf(stderr, "loop_seconds %.6f steps %d\n",
+                     std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(), in.tf);
+        put(out, pop.data(), (size_t)15 * n);
         put(out, populations(pg).data(), (size_t)15 * n);
         for (const double *p : std::vector<const double *>{rho.data(), pux, puy, puz, tem.data(), pqx, pqy, pqz})
             put(out, p, n);
