@@ -188,6 +188,11 @@ int pl_set_stream(pl_lattice h, void *stream);
  *                        a 16-bit ulp -- a small source added every step -- still accumulate in
  *                        expectation. Replayed graphs reuse their captured seeds. */
 #define PL_OPT_STOCHASTIC_ROUNDING 3
+/*  PL_OPT_SNAPSHOT_IN_STEP  1: every saving collide / step of a kind with a snapshot writes its
+ *                        snapshot slot in the same pass, so the pl_snapshot call that follows
+ *                        runs no kernel (for sweeps that take a snapshot at every step);
+ *                        0 (default): pl_snapshot re-evaluates the last collide's input state. */
+#define PL_OPT_SNAPSHOT_IN_STEP 4
 int pl_set_option(pl_lattice h, int option, int value);
 /* time-varying inflow (no counterpart in the reference, whose inflows are constant): the
  * prescribed velocity of every NS SetU / ANS iSetU op is multiplied by `scale` in the steps that

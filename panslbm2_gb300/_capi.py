@@ -28,7 +28,7 @@ BC_EL_STRESS, BC_AEL_STRESS = 15, 16
 SMOOTH_CORNER, SMOOTH_AT, SMOOTH_LINE = 20, 21, 22
 # fields
 ALPHA, KAPPA, BETA, DIRX, DIRY, DIRZ, DENSITY, GAMMA = 0, 1, 2, 3, 4, 5, 6, 7
-OPT_GRAPHS, OPT_SIDE_PRIORITY, OPT_STOCHASTIC_ROUNDING = 1, 2, 3
+OPT_GRAPHS, OPT_SIDE_PRIORITY, OPT_STOCHASTIC_ROUNDING, OPT_SNAPSHOT_IN_STEP = 1, 2, 3, 4
 RHO, UX, UY, UZ, TEM, QX, QY, QZ = 8, 9, 10, 11, 12, 13, 14, 15
 IP, IUX, IUY, IUZ, IMX, IMY, IMZ, ITEM, IQX, IQY, IQZ = 16, 17, 18, 19, 20, 21, 22, 23, 24, 25, 26
 FWD_RHO, FWD_UX, FWD_UY, FWD_UZ, FWD_TEM = 32, 33, 34, 35, 36

@@ -103,6 +103,8 @@ struct pl_lattice_s {
     std::vector<Program> progs;
     double *snap[2] = {nullptr, nullptr};
     bool snap_ok[2] = {false, false};   // the snapshot buffer holds a taken / loaded snapshot
+    bool snap_in_step = false;          // PL_OPT_SNAPSHOT_IN_STEP
+    bool snap_fresh[2] = {false, false};   // the last collide of the family wrote the snapshot
     // last collide, for snapshots
     int last_kind = -1, last_src = -1, last_prog = -1, last_pull = 0, last_bcu_slot = -1;
     pl_phys last_ph{};
@@ -699,15 +701,36 @@ void after_collide(pl_lattice h, int kind, bool save, int src, int prog, bool pu
     }
 }
 
+// a saving collide of a snapshot kind writes its snapshot itself when PL_OPT_SNAPSHOT_IN_STEP is set
+int snapshot_target(pl_lattice h, int kind, bool save, double **out) {
+    const int slot = pl::kind_is_adjoint(kind) ? 1 : 0;
+    *out = nullptr;
+    if (!(h->snap_in_step && save && pl::kind_has_snapshot(kind))) { h->snap_fresh[slot] = false; return PL_OK; }
+    int r = ensure_d(h, &h->snap[slot], (size_t)h->q * h->np);
+    if (r) return r;
+    *out = h->snap[slot];
+    return PL_OK;
+}
+void snapshot_taken(pl_lattice h, int kind, const double *snap) {
+    const int slot = pl::kind_is_adjoint(kind) ? 1 : 0;
+    h->snap_fresh[slot] = snap != nullptr;
+    if (snap) h->snap_ok[slot] = true;
+}
+
 int do_collide(pl_lattice h, int kind, const pl_phys *ph, bool save) {
     if (int e = check_kind(h, kind)) return e;
     const bool adjk = pl::kind_is_adjoint(kind);
     if (!adjk) save = true;   // boundary ops of the next step read this velocity
-    KArgs a;
-    int r = build_args(h, kind, ph, -1, h->cur, h->cur ^ 1, save, false, -1, a);
+    double *snap = nullptr;
+    int r = snapshot_target(h, kind, save, &snap);
     if (r) return r;
+    KArgs a;
+    r = build_args(h, kind, ph, -1, h->cur, h->cur ^ 1, save, false, -1, a);
+    if (r) return r;
+    a.snap_coll = snap;
     if (h->launch(kind, pl::OP_COLLIDE, save, a, h->st)) return fail(PL_ERR_UNSUPPORTED, "kind %d not built for this storage", kind);
     if ((r = check_launch(h, 1))) return r;
+    snapshot_taken(h, kind, snap);
     after_collide(h, kind, save, h->cur, -1, false, -1, ph);
     h->cur ^= 1;
     return PL_OK;
@@ -716,11 +739,16 @@ int do_collide(pl_lattice h, int kind, const pl_phys *ph, bool save) {
 int do_step(pl_lattice h, int kind, const pl_phys *ph, int prog, bool save) {
     if (int e = check_kind(h, kind)) return e;
     const int bcu_slot = h->fwd_latest;
-    KArgs a;
-    int r = build_args(h, kind, ph, prog, h->cur, h->cur ^ 1, save, true, bcu_slot, a);
+    double *snap = nullptr;
+    int r = snapshot_target(h, kind, save, &snap);
     if (r) return r;
+    KArgs a;
+    r = build_args(h, kind, ph, prog, h->cur, h->cur ^ 1, save, true, bcu_slot, a);
+    if (r) return r;
+    a.snap_coll = snap;
     if (h->launch(kind, pl::OP_STEP, save, a, h->st)) return fail(PL_ERR_UNSUPPORTED, "kind %d not built for this storage", kind);
     if ((r = check_launch(h, a.nb > 0 ? (a.staged ? 1 + (a.ndir > 0) + (a.ns > 0 ? 2 : 0) : 2) : 1))) return r;
+    snapshot_taken(h, kind, snap);
     after_collide(h, kind, save, h->cur, prog, true, bcu_slot, ph);
     h->cur ^= 1;
     return PL_OK;
@@ -944,6 +972,10 @@ int pl_set_option(pl_lattice h, int option, int value) {
     if (value != 0 && value != 1) return fail(PL_ERR_ARG, "option value must be 0 or 1");
     if (option == PL_OPT_GRAPHS) {
         h->use_graphs = value == 1;
+        return PL_OK;
+    }
+    if (option == PL_OPT_SNAPSHOT_IN_STEP) {
+        h->snap_in_step = value == 1;
         return PL_OK;
     }
     if (option == PL_OPT_STOCHASTIC_ROUNDING) {
@@ -1363,6 +1395,8 @@ int pl_snapshot(pl_lattice h, int slot, double *host) {
     if (!pl::kind_has_snapshot(h->last_kind)) return fail(PL_ERR_STATE, "kind %d stores no snapshot", h->last_kind);
     int r = ensure_d(h, &h->snap[slot], (size_t)h->q * h->np);
     if (r) return r;
+    if (h->snap_fresh[slot]) goto taken;   // the last collide wrote it (PL_OPT_SNAPSHOT_IN_STEP)
+    {
     // the last collide read population buffer last_src; re-evaluate its input state
     const int saved_next = pl::kind_is_adjoint(h->last_kind) ? h->adj_next : h->fwd_next;
     KArgs a;
@@ -1374,6 +1408,8 @@ int pl_snapshot(pl_lattice h, int slot, double *host) {
     a.snap = h->snap[slot];
     if (h->launch(h->last_kind, pl::OP_SNAPSHOT, false, a, h->st)) return fail(PL_ERR_UNSUPPORTED, "snapshot kind");
     if ((r = check_launch(h, 1))) return r;
+    }
+taken:
     h->snap_ok[slot] = true;
     if (host) {
         double *buf;
@@ -1394,6 +1430,7 @@ int pl_set_snapshot(pl_lattice h, int slot, const double *host) {
     if ((r = upload(h, buf, host, (size_t)h->q * h->n))) return r;
     pl::launch_node_major_to_snap(buf, h->np, h->n, h->q, h->snap[slot], h->st);
     h->snap_ok[slot] = true;
+    h->snap_fresh[slot] = false;
     return check_launch(h, 1);
 }
 
@@ -1547,6 +1584,7 @@ int pl_load(pl_lattice h, int what, int slot) {
     if (what == PL_STORE_POPS) {
         CK(cudaMemcpyAsync(h->pop[h->cur], src, store_bytes(h, what), cudaMemcpyDeviceToDevice, h->st));
         h->last_kind = -1;
+        h->snap_fresh[0] = h->snap_fresh[1] = false;
     } else if (what == PL_STORE_FWD) {
         for (int m = 0; m < 5; ++m) {
             const int f = PL_FWD_RHO + m;
@@ -1559,6 +1597,7 @@ int pl_load(pl_lattice h, int what, int slot) {
         if ((r = ensure_d(h, &h->snap[0], (size_t)h->q * h->np))) return r;
         CK(cudaMemcpyAsync(h->snap[0], src, store_bytes(h, what), cudaMemcpyDeviceToDevice, h->st));
         h->snap_ok[0] = true;
+        h->snap_fresh[0] = false;
     }
     return PL_OK;
 }
@@ -1579,6 +1618,7 @@ int pl_store_swap_snapshot(pl_lattice h, int slot) {
     v[slot] = h->snap[0];
     h->snap[0] = static_cast<double *>(t);
     const bool was_ok = h->snap_ok[0];
+    h->snap_fresh[0] = false;
     h->snap_ok[0] = h->snap_filled[slot] != 0;
     h->snap_filled[slot] = was_ok ? 1 : 0;
     return PL_OK;

@@ -120,7 +120,9 @@ struct KArgs {
                                 //  adjoint: ip,iux,iuy,iuz,imx,imy,imz,item,iqx,iqy,iqz;
                                 //  EL: ux,uy in 1,2 and sxx,sxy,syx,syy in 4..7;
                                 //  AEL: irho 0, imx,imy 4,5, isxx,isxy,isyx,isyy 7..10)
-    double *snap;               // pre-collision g snapshot, [q][np] planes
+    double *snap;               // pre-collision g snapshot, [q][np] planes (k_snapshot)
+    double *snap_coll;          // the same, written by a saving collide or step itself
+                                // (PL_OPT_SNAPSHOT_IN_STEP), else null
     // boundary program
     const int *bnode;           // boundary nodes (sorted)
     const int *bstart;          // CSR op offsets per boundary node

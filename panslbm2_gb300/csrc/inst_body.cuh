@@ -15,29 +15,29 @@ using TC = Store<PL_STORE>::T;
 // collide of a runtime kind (uniform over the grid), for the boundary kernels
 static __device__ __forceinline__ void collide_any(int kind, TC *f, TC *g, int idx, const KArgs &a, bool save, TC *u) {
     switch (kind) {
-    case K_AD_NATURAL: collide_node<PL_LAT, TC, K_AD_NATURAL>(f, g, idx, a, save, nullptr, a.geo.np, u); break;
-    case K_AD_FORCE: collide_node<PL_LAT, TC, K_AD_FORCE>(f, g, idx, a, save, nullptr, a.geo.np, u); break;
-    case K_AAD_NATURAL: collide_node<PL_LAT, TC, K_AAD_NATURAL>(f, g, idx, a, save, nullptr, a.geo.np, nullptr); break;
-    case K_AAD_FORCE: collide_node<PL_LAT, TC, K_AAD_FORCE>(f, g, idx, a, save, nullptr, a.geo.np, nullptr); break;
-    case K_NS_COLLIDE: collide_node<PL_LAT, TC, K_NS_COLLIDE>(f, g, idx, a, save, nullptr, a.geo.np, u); break;
+    case K_AD_NATURAL: collide_node<PL_LAT, TC, K_AD_NATURAL>(f, g, idx, a, save, a.snap_coll, a.geo.np, u); break;
+    case K_AD_FORCE: collide_node<PL_LAT, TC, K_AD_FORCE>(f, g, idx, a, save, a.snap_coll, a.geo.np, u); break;
+    case K_AAD_NATURAL: collide_node<PL_LAT, TC, K_AAD_NATURAL>(f, g, idx, a, save, a.snap_coll, a.geo.np, nullptr); break;
+    case K_AAD_FORCE: collide_node<PL_LAT, TC, K_AAD_FORCE>(f, g, idx, a, save, a.snap_coll, a.geo.np, nullptr); break;
+    case K_NS_COLLIDE: collide_node<PL_LAT, TC, K_NS_COLLIDE>(f, g, idx, a, save, a.snap_coll, a.geo.np, u); break;
 #ifdef PL_ALL_KINDS
-    case K_NS_BRINKMAN: collide_node<PL_LAT, TC, K_NS_BRINKMAN>(f, g, idx, a, save, nullptr, a.geo.np, u); break;
-    case K_AD_HEATEX: collide_node<PL_LAT, TC, K_AD_HEATEX>(f, g, idx, a, save, nullptr, a.geo.np, u); break;
-    case K_AD_NATURAL_NOBRINK: collide_node<PL_LAT, TC, K_AD_NATURAL_NOBRINK>(f, g, idx, a, save, nullptr, a.geo.np, u); break;
-    case K_AD_FORCE_NOBRINK: collide_node<PL_LAT, TC, K_AD_FORCE_NOBRINK>(f, g, idx, a, save, nullptr, a.geo.np, u); break;
-    case K_ANS_BRINKMAN: collide_node<PL_LAT, TC, K_ANS_BRINKMAN>(f, g, idx, a, save, nullptr, a.geo.np, nullptr); break;
-    case K_AAD_HEATEX: collide_node<PL_LAT, TC, K_AAD_HEATEX>(f, g, idx, a, save, nullptr, a.geo.np, nullptr); break;
-    case K_AAD_MASSFLOW: collide_node<PL_LAT, TC, K_AAD_MASSFLOW>(f, g, idx, a, save, nullptr, a.geo.np, nullptr); break;
+    case K_NS_BRINKMAN: collide_node<PL_LAT, TC, K_NS_BRINKMAN>(f, g, idx, a, save, a.snap_coll, a.geo.np, u); break;
+    case K_AD_HEATEX: collide_node<PL_LAT, TC, K_AD_HEATEX>(f, g, idx, a, save, a.snap_coll, a.geo.np, u); break;
+    case K_AD_NATURAL_NOBRINK: collide_node<PL_LAT, TC, K_AD_NATURAL_NOBRINK>(f, g, idx, a, save, a.snap_coll, a.geo.np, u); break;
+    case K_AD_FORCE_NOBRINK: collide_node<PL_LAT, TC, K_AD_FORCE_NOBRINK>(f, g, idx, a, save, a.snap_coll, a.geo.np, u); break;
+    case K_ANS_BRINKMAN: collide_node<PL_LAT, TC, K_ANS_BRINKMAN>(f, g, idx, a, save, a.snap_coll, a.geo.np, nullptr); break;
+    case K_AAD_HEATEX: collide_node<PL_LAT, TC, K_AAD_HEATEX>(f, g, idx, a, save, a.snap_coll, a.geo.np, nullptr); break;
+    case K_AAD_MASSFLOW: collide_node<PL_LAT, TC, K_AAD_MASSFLOW>(f, g, idx, a, save, a.snap_coll, a.geo.np, nullptr); break;
 #endif
 #if defined(PL_ALL_KINDS) && defined(PL_INCOMPRESSIBLE)
-    case K_NSIN_COLLIDE: collide_node<PL_LAT, TC, K_NSIN_COLLIDE>(f, g, idx, a, save, nullptr, a.geo.np, u); break;
-    case K_NSIN_BRINKMAN: collide_node<PL_LAT, TC, K_NSIN_BRINKMAN>(f, g, idx, a, save, nullptr, a.geo.np, u); break;
-    case K_ANSIN_BRINKMAN: collide_node<PL_LAT, TC, K_ANSIN_BRINKMAN>(f, g, idx, a, save, nullptr, a.geo.np, nullptr); break;
+    case K_NSIN_COLLIDE: collide_node<PL_LAT, TC, K_NSIN_COLLIDE>(f, g, idx, a, save, a.snap_coll, a.geo.np, u); break;
+    case K_NSIN_BRINKMAN: collide_node<PL_LAT, TC, K_NSIN_BRINKMAN>(f, g, idx, a, save, a.snap_coll, a.geo.np, u); break;
+    case K_ANSIN_BRINKMAN: collide_node<PL_LAT, TC, K_ANSIN_BRINKMAN>(f, g, idx, a, save, a.snap_coll, a.geo.np, nullptr); break;
 #endif
 #if defined(PL_ALL_KINDS) && defined(PL_ELASTIC)
-    case K_EL_COLLIDE: collide_node<PL_LAT, TC, K_EL_COLLIDE>(f, g, idx, a, save, nullptr, a.geo.np, u); break;
-    case K_EL_EXTENDED: collide_node<PL_LAT, TC, K_EL_EXTENDED>(f, g, idx, a, save, nullptr, a.geo.np, u); break;
-    case K_AEL_COLLIDE: collide_node<PL_LAT, TC, K_AEL_COLLIDE>(f, g, idx, a, save, nullptr, a.geo.np, nullptr); break;
+    case K_EL_COLLIDE: collide_node<PL_LAT, TC, K_EL_COLLIDE>(f, g, idx, a, save, a.snap_coll, a.geo.np, u); break;
+    case K_EL_EXTENDED: collide_node<PL_LAT, TC, K_EL_EXTENDED>(f, g, idx, a, save, a.snap_coll, a.geo.np, u); break;
+    case K_AEL_COLLIDE: collide_node<PL_LAT, TC, K_AEL_COLLIDE>(f, g, idx, a, save, a.snap_coll, a.geo.np, nullptr); break;
 #endif
     default: break;
     }

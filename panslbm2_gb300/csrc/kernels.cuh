@@ -122,7 +122,7 @@ __device__ __forceinline__ void node_tail(const KArgs &a, int idx, int code, typ
         }
     }
     T u[3];
-    collide_node<L, T, K>(f, g, idx, a, a.save != 0, nullptr, a.geo.np, (INL && !kind_is_adjoint(K)) ? u : nullptr);
+    collide_node<L, T, K>(f, g, idx, a, a.save != 0, a.snap_coll, a.geo.np, (INL && !kind_is_adjoint(K)) ? u : nullptr);
     if constexpr (INL && !kind_is_adjoint(K)) {
         if (code >= 0 && a.bcu_out[0]) {
             a.bcu_out[0][idx] = double(u[0]);
@@ -230,7 +230,7 @@ __global__ void __launch_bounds__(128) k_boundary(KArgs a) {
     T f[L::Q], g[L::Q];
     eval_node<L, S, 4>(a, idx, 0x7fffffff, f, g, HG, kind_is_adjoint(K) ? 1 : -1);
     T u[3];
-    collide_node<L, T, K>(f, g, idx, a, a.save != 0, nullptr, a.geo.np, !kind_is_adjoint(K) ? u : nullptr);
+    collide_node<L, T, K>(f, g, idx, a, a.save != 0, a.snap_coll, a.geo.np, !kind_is_adjoint(K) ? u : nullptr);
     if (!kind_is_adjoint(K) && a.bcu_out[0]) {
         a.bcu_out[0][idx] = double(u[0]);
         a.bcu_out[1][idx] = double(u[1]);

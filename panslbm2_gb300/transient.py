@@ -49,6 +49,8 @@ class TransientHeatSink:
         self.q = 9 if p.nd == 2 else 15
         self.n = p.lx * p.ly * p.lz
         self.lp = LatticePair(self.q, p.lx, p.ly, p.lz, storage)
+        # every step of the sweep takes its snapshot: write it in the step's own pass
+        self.lp.set_option(A.OPT_SNAPSHOT_IN_STEP, 1)
         if self.forced:
             self.kf, self.ka = A.AD_FORCE, A.AAD_FORCE
             self.prog_f = self.lp.program(HS.to_descs(p.program_ops("forward")))
