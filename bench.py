@@ -255,7 +255,7 @@ def cavity_leg():
             "max_rel_diff_gpu_vs_cpu": diff}
 
 
-def design_leg(cpu=True, cpu_budget_s=45.0):
+def design_leg(cpu=True, cpu_budget_s=120.0):
     """config 2: one forced-convection design iteration on 200x100 FP64 (filter, forward and
     adjoint to 1e-6, sensitivity, filtered sensitivity); the CPU port's forward + adjoint on the
     same step counts"""
