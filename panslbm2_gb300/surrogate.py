@@ -210,13 +210,16 @@ class SurrogateWarmStart:
         self.hs.close()
         self.net.close()
 
-    def generate(self, count, first_seed=1000, tol=1e-6, max_steps=100000, max_adjoint_steps=40000, log=None):
+    def generate(self, count, first_seed=1000, tol=1e-6, max_steps=100000, max_adjoint_steps=40000, log=None,
+                 max_seconds=None):
         """solve seeded designs first_seed, first_seed + 1, ... to `tol` until `count` pairs whose
-        forward and adjoint both converged are stored (the others are skipped and logged);
-        returns the per-design records"""
+        forward and adjoint both converged are stored (the others are skipped and logged), or
+        until max_seconds of wall time have passed; returns the per-design records (the number
+        stored is the count of records with used = True)"""
         self.net.reserve(count)
         info, slot, sd = [], 0, first_seed
-        while slot < count:
+        start = time.perf_counter()
+        while slot < count and (max_seconds is None or time.perf_counter() - start < max_seconds):
             t0 = time.perf_counter()
             s = self.p.design(seed=sd)
             ss, (stf, nf), (sta, na) = self.hs.solve_pair(s, tol, max_steps, max_adjoint_steps)
@@ -301,7 +304,10 @@ def main(argv=None):
     ap.add_argument("--base", type=int, default=16)
     ap.add_argument("--out", required=True)
     ap.add_argument("--log", default=None)
-    ap.add_argument("--eval-seed", type=int, default=0)
+    ap.add_argument("--eval-seeds", default="0,1,2,3,4",
+                    help="held-out designs of the cold / warm-started comparison")
+    ap.add_argument("--max-generate-s", type=float, default=None,
+                    help="stop generating after this many seconds and train on the pairs stored")
     ap.add_argument("--max-adjoint-steps", type=int, default=25000,
                     help="training designs whose adjoint does not converge within this are skipped")
     a = ap.parse_args(argv)
@@ -318,28 +324,37 @@ def main(argv=None):
     t0 = time.perf_counter()
     rec["samples"] = sw.generate(a.nsamples, a.first_seed, tol=a.data_tol or a.tol,
                                  max_adjoint_steps=a.max_adjoint_steps,
-                                 log=lambda d: (log.append(d), out(dict(sample=d))))
+                                 log=lambda d: (log.append(d), out(dict(sample=d))),
+                                 max_seconds=a.max_generate_s)
     rec["generate_s"] = round(time.perf_counter() - t0, 2)
     used = [d["seed"] for d in rec["samples"] if d["used"]]
+    nstored = len(used)
+    if nstored == 0:
+        raise SystemExit("no training design converged")
+    rec["nsamples"] = nstored
     rec["seeds"] = [min(used), max(used)]
     rec["skipped_seeds"] = [d["seed"] for d in rec["samples"] if not d["used"]]
     t1 = time.perf_counter()
-    loss = sw.train(a.nsamples, a.epochs, a.batch, a.lr, seed=7)
+    loss = sw.train(nstored, a.epochs, a.batch, a.lr, seed=7)
     sw.hs.lp.synchronize()
     rec["train_s"] = round(time.perf_counter() - t1, 2)
     rec["loss"] = [float(v) for v in loss]
-    out(dict(loss=rec["loss"], train_s=rec["train_s"]))
-    sw.net.save(a.out, meta=dict(nsamples=a.nsamples, epochs=a.epochs, seeds=rec["seeds"],
+    out(dict(loss=rec["loss"], train_s=rec["train_s"], nsamples=nstored))
+    sw.net.save(a.out, meta=dict(nsamples=nstored, epochs=a.epochs, seeds=rec["seeds"],
                                  skipped=rec["skipped_seeds"], data_tol=a.data_tol or a.tol))
-    s = p.design(seed=a.eval_seed)
-    ev = {}
-    for name, warm in (("plain", False), ("surrogate", True), ("plain_again", False), ("surrogate_again", True)):
-        r = sw.iterate(s, warm, tol=a.tol)
-        ev[name] = dict(seconds=round(r["seconds"]["total"], 3), phases={k: round(v, 3) for k, v in r["seconds"].items()},
-                        forward_steps=r["forward"][1], adjoint_steps=r["adjoint"][1],
-                        converged=[r["forward"][0] == A.PL_CONVERGED, r["adjoint"][0] == A.PL_CONVERGED],
-                        objective=r["objective"])
-        out(dict(eval=name, **ev[name]))
+    ev = []
+    for sd in (int(v) for v in a.eval_seeds.split(",")):
+        s = p.design(seed=sd)
+        row = dict(seed=sd)
+        for name, warm in (("plain", False), ("surrogate", True)):
+            r = sw.iterate(s, warm, tol=a.tol)
+            row[name] = dict(seconds=round(r["seconds"]["total"], 3),
+                             phases={k: round(v, 3) for k, v in r["seconds"].items()},
+                             forward_steps=r["forward"][1], adjoint_steps=r["adjoint"][1],
+                             converged=[r["forward"][0] == A.PL_CONVERGED, r["adjoint"][0] == A.PL_CONVERGED],
+                             objective=r["objective"])
+        out(dict(eval=row))
+        ev.append(row)
     rec["eval"] = ev
     if a.log:
         with open(a.log, "w") as fh:
