@@ -451,11 +451,13 @@ int compile_program(pl_lattice h, const pl_bc_desc *descs, int ndesc, Program &P
                 for (int o = bstart[sl]; o < bstart[sl + 1]; ++o) {
                     const Op &op = ops[o];
                     const int m = o - bstart[sl];
-                    const uint32_t b = (uint32_t)pl::simple_index(op.kind) | ((uint32_t)op.axis << 3) |
-                                       (op.dir > 0 ? 32u : 0u) | (op.lat ? 64u : 0u) | (op.sub == 2 ? 128u : 0u);
-                    rec.code |= b << (8 * m);
-                    rec.v[m] = (op.kind == pl::BC_AAD_Q) ? op.eps : op.v0;
-                    rec.w[m] = op.v1;
+                    const uint64_t b = (uint64_t)pl::simple_index(op.kind) | ((uint64_t)op.axis << 4) |
+                                       (op.dir > 0 ? 64u : 0u) | (op.lat ? 128u : 0u) | (op.sub == 2 ? 256u : 0u);
+                    rec.code |= b << (16 * m);
+                    rec.val[m][0] = (op.kind == pl::BC_AAD_Q) ? op.eps : op.v0;
+                    rec.val[m][1] = op.v1;
+                    rec.val[m][2] = op.v2;
+                    rec.val[m][3] = op.eps;
                 }
                 rec.nops = (uint32_t)(bstart[sl + 1] - bstart[sl]);
                 icode[node] = (int)irec.size();

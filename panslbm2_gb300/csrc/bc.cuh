@@ -69,6 +69,140 @@ __device__ __forceinline__ void tang3(int a, int &t0, int &t1) {
     t1 = a == 0 ? 2 : (a == 1 ? 0 : 1);
 }
 
+// NS::BoundaryConditionSetU / SetRho on face (A, D) (navierstokes.h:90-426). setu: val = the
+// velocity (inflow scale applied); else val[0] = rho and val[1], val[2] the tangential velocity.
+// A and D are compile-time constants: the interior kernel calls this for its face nodes and
+// apply_op dispatches to it over the six faces, so both paths run the same arithmetic.
+template <class L, class T, int A, int D>
+__device__ __forceinline__ void ns_face_ud(bool setu, const T *val, T *p) {
+    constexpr int Q = L::Q, ND = L::ND;
+    T u[3] = {T(0), T(0), T(0)};
+    T sT = T(0), sO = T(0);
+    bool first = true;
+#pragma unroll
+    for (int c = 0; c < Q; ++c)
+        if (cmp<L>(c, A) == 0) { if (first) { sT = p[c]; first = false; } else sT += p[c]; }
+    first = true;
+#pragma unroll
+    for (int c = 0; c < Q; ++c)
+        if (cmp<L>(c, A) == D) { if (first) { sO = p[c]; first = false; } else sO += p[c]; }
+    const T S = sT + T(2) * sO;
+    T rho0;
+    if (setu) {
+        u[0] = val[0]; u[1] = val[1]; if (ND == 3) u[2] = val[2];
+        rho0 = S / (D < 0 ? T(1) - u[A] : T(1) + u[A]);
+    } else {
+        rho0 = val[0];
+        if (ND == 2) u[1 - A] = val[1];
+        else { u[(A + 1) % 3] = val[1]; u[(A + 2) % 3] = val[2]; }
+        u[A] = D < 0 ? T(1) - S / rho0 : T(-1) + S / rho0;
+    }
+    const T kn = ND == 2 ? T(6) : T(12), kt = ND == 2 ? T(0.5) : T(0.25), kc = ND == 2 ? T(4) : T(8);
+    T m[3];
+#pragma unroll
+    for (int b = 0; b < ND; ++b) {
+        if (b == A) m[b] = rho0 * u[b] / kn;
+        else {
+            T fp = T(0), fm = T(0);
+#pragma unroll
+            for (int c = 1; c < Q; ++c) {
+                if (diag_of<L>(c, b)) continue;
+                if (cmp<L>(c, b) == 1) fp = p[c];
+                if (cmp<L>(c, b) == -1) fm = p[c];
+            }
+            m[b] = kt * (fp - fm - rho0 * u[b]);
+        }
+    }
+    T src[Q];
+#pragma unroll
+    for (int c = 0; c < Q; ++c) src[c] = p[c];
+#pragma unroll
+    for (int c = 1; c < Q; ++c) {
+        if (cmp<L>(c, A) != -D) continue;
+        T v = src[opp_d<L>(c)];
+        if (!diag_of<L>(c, A)) {
+            v = cmp<L>(c, A) > 0 ? v + kc * m[A] : v - kc * m[A];
+        } else {
+#pragma unroll
+            for (int b = 0; b < ND; ++b) {
+                const int cb = cmp<L>(c, b);
+                if (b == A) v = cb > 0 ? v + m[b] : v - m[b];
+                else v = cb > 0 ? v - m[b] : v + m[b];
+            }
+        }
+        p[c] = v;
+    }
+}
+
+// ANS::iBoundaryConditionSetU / SetRho on face (A, D) (adjointnavierstokes.h:95-392); u the
+// velocity (inflow scale applied), eps the objective weight of the edge
+template <class L, class T, int A, int D>
+__device__ __forceinline__ void ans_face_ud(bool setu, T eps, const T *u, T *p) {
+    constexpr int Q = L::Q, ND = L::ND;
+    T rho0;
+    if (!setu) {
+        rho0 = nsum<L, T>(p, A, D, ND == 2 ? T(4) : T(8)) / (ND == 2 ? T(3) : T(6));
+        T src[Q];
+#pragma unroll
+        for (int c = 0; c < Q; ++c) src[c] = p[c];
+#pragma unroll
+        for (int c = 1; c < Q; ++c) if (cmp<L>(c, A) == D) p[c] = src[opp_d<L>(c)] - rho0;
+        return;
+    }
+    if (ND == 2) {
+        const T un = u[0], ut = A == 0 ? u[1] : u[0];   // y edges use ux twice (reference)
+        constexpr int B = 1 - A;
+        const T ns = nsum<L, T>(p, A, D, T(4));
+        const T ts = tsum<L, T>(p, A, D, B);
+        T num = D < 0 ? T(-2) * eps + un * ns : T(-2) * eps - un * ns;
+        num += T(3) * ut * ts;
+        rho0 = num / (T(3) * (D < 0 ? T(1) - un : T(1) + un));
+    } else {
+        T num = T(-4) * eps;
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+            if (b == A) {
+                const T ns = nsum<L, T>(p, A, D, T(8));
+                num = D < 0 ? num + u[A] * ns : num - u[A] * ns;
+            } else {
+                num += T(3) * u[b] * tsum<L, T>(p, A, D, b);
+            }
+        }
+        rho0 = num / (T(6) * (D < 0 ? T(1) - u[A] : T(1) + u[A]));
+    }
+    T src[Q];
+#pragma unroll
+    for (int c = 0; c < Q; ++c) src[c] = p[c];
+#pragma unroll
+    for (int c = 1; c < Q; ++c) if (cmp<L>(c, A) == D) p[c] = src[opp_d<L>(c)] + rho0;
+}
+
+// runtime face -> the face-templated NS / ANS routine
+template <class L, class T>
+__device__ __forceinline__ void ns_ud(int A, int d, bool setu, const T *val, T *p) {
+    switch (A * 2 + (d > 0 ? 1 : 0)) {
+    case 0: ns_face_ud<L, T, 0, -1>(setu, val, p); break;
+    case 1: ns_face_ud<L, T, 0, 1>(setu, val, p); break;
+    case 2: ns_face_ud<L, T, 1, -1>(setu, val, p); break;
+    case 3: ns_face_ud<L, T, 1, 1>(setu, val, p); break;
+    case 4: if (L::ND == 3) ns_face_ud<L, T, 2, -1>(setu, val, p); break;
+    case 5: if (L::ND == 3) ns_face_ud<L, T, 2, 1>(setu, val, p); break;
+    default: break;
+    }
+}
+template <class L, class T>
+__device__ __forceinline__ void ans_ud(int A, int d, bool setu, T eps, const T *u, T *p) {
+    switch (A * 2 + (d > 0 ? 1 : 0)) {
+    case 0: ans_face_ud<L, T, 0, -1>(setu, eps, u, p); break;
+    case 1: ans_face_ud<L, T, 0, 1>(setu, eps, u, p); break;
+    case 2: ans_face_ud<L, T, 1, -1>(setu, eps, u, p); break;
+    case 3: ans_face_ud<L, T, 1, 1>(setu, eps, u, p); break;
+    case 4: if (L::ND == 3) ans_face_ud<L, T, 2, -1>(setu, eps, u, p); break;
+    case 5: if (L::ND == 3) ans_face_ud<L, T, 2, 1>(setu, eps, u, p); break;
+    default: break;
+    }
+}
+
 // wall copy on one population set; every array index is a compile-time constant after
 // unrolling (the runtime axis only selects among constants), so the set stays in registers
 template <class L, class T>
@@ -102,65 +236,14 @@ __device__ __forceinline__ void apply_op(const Op &op, T *f, T *g, int node, con
     }
     case BC_NS_U:
     case BC_NS_RHO: if constexpr (!SIMPLE) {
-        T *p = f;
-        T u[3] = {T(0), T(0), T(0)};
-        T sT = T(0), sO = T(0);
-        bool first = true;
-#pragma unroll
-        for (int c = 0; c < Q; ++c)
-            if (cmp<L>(c, A) == 0) { if (first) { sT = p[c]; first = false; } else sT += p[c]; }
-        first = true;
-#pragma unroll
-        for (int c = 0; c < Q; ++c)
-            if (cmp<L>(c, A) == d) { if (first) { sO = p[c]; first = false; } else sO += p[c]; }
-        const T S = sT + T(2) * sO;
-        T rho0;
+        T val[3];
         if (op.kind == BC_NS_U) {
             // uscale: time-varying inflow u(t) = uscale * u (1 = the reference routine)
-            u[0] = T(a.uscale * op.v0); u[1] = T(a.uscale * op.v1); if (ND == 3) u[2] = T(a.uscale * op.v2);
-            rho0 = S / (d < 0 ? T(1) - u[A] : T(1) + u[A]);
+            val[0] = T(a.uscale * op.v0); val[1] = T(a.uscale * op.v1); val[2] = ND == 3 ? T(a.uscale * op.v2) : T(0);
         } else {
-            rho0 = T(op.v0);
-            if (ND == 2) u[1 - A] = T(op.v1);
-            else { u[(A + 1) % 3] = T(op.v1); u[(A + 2) % 3] = T(op.v2); }
-            u[A] = d < 0 ? T(1) - S / rho0 : T(-1) + S / rho0;
+            val[0] = T(op.v0); val[1] = T(op.v1); val[2] = ND == 3 ? T(op.v2) : T(0);
         }
-        const T kn = ND == 2 ? T(6) : T(12), kt = ND == 2 ? T(0.5) : T(0.25), kc = ND == 2 ? T(4) : T(8);
-        T m[3];
-#pragma unroll
-        for (int b = 0; b < ND; ++b) {
-            if (b == A) m[b] = rho0 * u[b] / kn;
-            else {
-                T fp = T(0), fm = T(0);
-#pragma unroll
-                for (int c = 1; c < Q; ++c) {
-                    if (diag_of<L>(c, b)) continue;
-                    if (cmp<L>(c, b) == 1) fp = p[c];
-                    if (cmp<L>(c, b) == -1) fm = p[c];
-                }
-                m[b] = kt * (fp - fm - rho0 * u[b]);
-            }
-        }
-        T src[Q];
-#pragma unroll
-        for (int c = 0; c < Q; ++c) src[c] = p[c];
-#pragma unroll
-        for (int c = 1; c < Q; ++c) {
-            if (cmp<L>(c, A) != -d) continue;
-            T v = src[opp_d<L>(c)];
-            if (!diag_of<L>(c, A)) {
-                v = cmp<L>(c, A) > 0 ? v + kc * m[A] : v - kc * m[A];
-            } else {
-#pragma unroll
-                for (int b = 0; b < ND; ++b) {
-                    const int cb = cmp<L>(c, b);
-                    if (b == A) v = cb > 0 ? v + m[b] : v - m[b];
-                    else v = cb > 0 ? v - m[b] : v + m[b];
-                }
-            }
-            p[c] = v;
-        }
-        break;
+        ns_ud<L, T>(A, d, op.kind == BC_NS_U, val, f);
     } break;
     case BC_AD_T:
     case BC_AD_Q:
@@ -189,45 +272,8 @@ __device__ __forceinline__ void apply_op(const Op &op, T *f, T *g, int node, con
     }
     case BC_ANS_U:
     case BC_ANS_RHO: if constexpr (!SIMPLE) {
-        T *p = f;
-        T rho0;
-        if (op.kind == BC_ANS_RHO) {
-            rho0 = nsum<L, T>(p, A, d, ND == 2 ? T(4) : T(8)) / (ND == 2 ? T(3) : T(6));
-            T src[Q];
-#pragma unroll
-            for (int c = 0; c < Q; ++c) src[c] = p[c];
-#pragma unroll
-            for (int c = 1; c < Q; ++c) if (cmp<L>(c, A) == d) p[c] = src[opp_d<L>(c)] - rho0;
-            break;
-        }
         const T u[3] = {T(a.uscale * op.v0), T(a.uscale * op.v1), ND == 3 ? T(a.uscale * op.v2) : T(0)};
-        if (ND == 2) {
-            const T un = u[0], ut = A == 0 ? u[1] : u[0];   // y edges use ux twice (reference)
-            const int b = 1 - A;
-            const T ns = nsum<L, T>(p, A, d, T(4));
-            const T ts = tsum<L, T>(p, A, d, b);
-            T num = d < 0 ? T(-2) * T(op.eps) + un * ns : T(-2) * T(op.eps) - un * ns;
-            num += T(3) * ut * ts;
-            rho0 = num / (T(3) * (d < 0 ? T(1) - un : T(1) + un));
-        } else {
-            T num = T(-4) * T(op.eps);
-#pragma unroll
-            for (int b = 0; b < 3; ++b) {
-                if (b == A) {
-                    const T ns = nsum<L, T>(p, A, d, T(8));
-                    num = d < 0 ? num + u[A] * ns : num - u[A] * ns;
-                } else {
-                    num += T(3) * u[b] * tsum<L, T>(p, A, d, b);
-                }
-            }
-            rho0 = num / (T(6) * (d < 0 ? T(1) - u[A] : T(1) + u[A]));
-        }
-        T src[Q];
-#pragma unroll
-        for (int c = 0; c < Q; ++c) src[c] = p[c];
-#pragma unroll
-        for (int c = 1; c < Q; ++c) if (cmp<L>(c, A) == d) p[c] = src[opp_d<L>(c)] + rho0;
-        break;
+        ans_ud<L, T>(A, d, op.kind == BC_ANS_U, T(op.eps), u, f);
     } break;
     case BC_AAD_T:
     case BC_AAD_Q: {
@@ -432,9 +478,12 @@ __device__ __noinline__ void apply_op_ni(const Op &op, T *f, T *g, int node, con
 // ---- simple ops specialised on the face (axis A, side D) ---------------------------------------
 // Same arithmetic as apply_op; with A and D known at compile time every direction test folds,
 // leaving straight-line code. Used by the interior kernel for boundary nodes.
+// vals: the op's values (InlineRec::val); uscale the inflow scale of NS SetU / ANS iSetU.
 template <class L, class T, int A, int D>
-__device__ __forceinline__ void simple_face_op(int sk, int lat, int type, T v0, T v1, T *f, T *g, const T *u, T kp) {
+__device__ __forceinline__ void simple_face_op(int sk, int lat, int type, const double *vals, double uscale, T *f,
+                                               T *g, const T *u, T kp) {
     constexpr int Q = L::Q, ND = L::ND, NIN = -D;
+    const T v0 = T(vals[0]), v1 = T(vals[1]);
     switch (sk) {
     case 0:   // BC_WALL
     case 1: { // BC_IWALL
@@ -518,22 +567,36 @@ __device__ __forceinline__ void simple_face_op(int sk, int lat, int type, T v0, 
         for (int c = 1; c < Q; ++c) if (comp<L>(c, A) == D) g[c] = rho0;
         break;
     }
+    case 7:   // BC_NS_U
+    case 8: { // BC_NS_RHO
+        T val[3];
+        if (sk == 7) { val[0] = T(uscale * vals[0]); val[1] = T(uscale * vals[1]); val[2] = ND == 3 ? T(uscale * vals[2]) : T(0); }
+        else { val[0] = T(vals[0]); val[1] = T(vals[1]); val[2] = ND == 3 ? T(vals[2]) : T(0); }
+        ns_face_ud<L, T, A, D>(sk == 7, val, f);
+        break;
+    }
+    case 9:    // BC_ANS_U
+    case 10: { // BC_ANS_RHO
+        const T uu[3] = {T(uscale * vals[0]), T(uscale * vals[1]), ND == 3 ? T(uscale * vals[2]) : T(0)};
+        ans_face_ud<L, T, A, D>(sk == 9, T(vals[3]), uu, f);
+        break;
+    }
     default:
         break;
     }
 }
 
 template <class L, class T>
-__device__ __forceinline__ void simple_op(int axis, int dir, int sk, int lat, int type, T v0, T v1, T *f, T *g,
-                                          const T *u, T kp) {
+__device__ __forceinline__ void simple_op(int axis, int dir, int sk, int lat, int type, const double *vals,
+                                          double uscale, T *f, T *g, const T *u, T kp) {
     const int face = axis * 2 + (dir > 0 ? 1 : 0);
     switch (face) {
-    case 0: simple_face_op<L, T, 0, -1>(sk, lat, type, v0, v1, f, g, u, kp); break;
-    case 1: simple_face_op<L, T, 0, 1>(sk, lat, type, v0, v1, f, g, u, kp); break;
-    case 2: simple_face_op<L, T, 1, -1>(sk, lat, type, v0, v1, f, g, u, kp); break;
-    case 3: simple_face_op<L, T, 1, 1>(sk, lat, type, v0, v1, f, g, u, kp); break;
-    case 4: if (L::ND == 3) simple_face_op<L, T, 2, -1>(sk, lat, type, v0, v1, f, g, u, kp); break;
-    case 5: if (L::ND == 3) simple_face_op<L, T, 2, 1>(sk, lat, type, v0, v1, f, g, u, kp); break;
+    case 0: simple_face_op<L, T, 0, -1>(sk, lat, type, vals, uscale, f, g, u, kp); break;
+    case 1: simple_face_op<L, T, 0, 1>(sk, lat, type, vals, uscale, f, g, u, kp); break;
+    case 2: simple_face_op<L, T, 1, -1>(sk, lat, type, vals, uscale, f, g, u, kp); break;
+    case 3: simple_face_op<L, T, 1, 1>(sk, lat, type, vals, uscale, f, g, u, kp); break;
+    case 4: if (L::ND == 3) simple_face_op<L, T, 2, -1>(sk, lat, type, vals, uscale, f, g, u, kp); break;
+    case 5: if (L::ND == 3) simple_face_op<L, T, 2, 1>(sk, lat, type, vals, uscale, f, g, u, kp); break;
     default: break;
     }
 }

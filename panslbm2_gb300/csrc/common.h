@@ -44,29 +44,26 @@ enum BcKind {
     BC_SMOOTH = 20
 };
 
-// ops the interior kernel applies inline (walls, AD SetT / SetQ, AAD iSetT / iSetQ)
+// ops the interior kernel applies inline (walls, NS SetU / SetRho, AD SetT / SetQ, ANS iSetU /
+// iSetRho, AAD iSetT / iSetQ)
 __host__ __device__ constexpr bool op_is_simple(int k) {
     return k == BC_WALL || k == BC_IWALL || k == BC_AD_T || k == BC_AD_Q || k == BC_AD_QC || k == BC_AAD_T ||
-           k == BC_AAD_Q;
+           k == BC_AAD_Q || k == BC_NS_U || k == BC_NS_RHO || k == BC_ANS_U || k == BC_ANS_RHO;
 }
 
 // Compact record of the simple ops of one boundary node, read by the interior kernel in one
-// round trip: op m is byte m of `code` (bits 0-2 simple kind index, 3-4 axis, 5 side (+1 when
-// set), 6 set (g when set), 7 wall type (MIRROR when set)); v[m] its value (T / qn / eps) and
-// w[m] its second value (constant kappa).
+// round trip: op m is bits 16m..16m+15 of `code` (bits 0-3 simple kind index, 4-5 axis, 6 side
+// (+1 when set), 7 set (g when set), 8 wall type (MIRROR when set)); val[m] its values:
+// [0] T / qn / eps (AAD iSetQ) / u_x / rho, [1] constant kappa / u_y, [2] u_z, [3] eps (ANS).
 struct InlineRec {
-    uint32_t code, nops;
-    double v[4], w[4];
-    uint64_t pad;
+    uint64_t code;
+    uint32_t nops, pad;
+    double val[4][4];
 };
 constexpr int kInlineMaxOps = 4;
-__host__ __device__ constexpr int simple_kind(int idx) {
-    return idx == 0 ? BC_WALL : idx == 1 ? BC_IWALL : idx == 2 ? BC_AD_T : idx == 3 ? BC_AD_Q : idx == 4 ? BC_AD_QC
-         : idx == 5 ? BC_AAD_T : BC_AAD_Q;
-}
 __host__ __device__ constexpr int simple_index(int k) {
     return k == BC_WALL ? 0 : k == BC_IWALL ? 1 : k == BC_AD_T ? 2 : k == BC_AD_Q ? 3 : k == BC_AD_QC ? 4
-         : k == BC_AAD_T ? 5 : 6;
+         : k == BC_AAD_T ? 5 : k == BC_AAD_Q ? 6 : k == BC_NS_U ? 7 : k == BC_NS_RHO ? 8 : k == BC_ANS_U ? 9 : 10;
 }
 
 // One boundary-program op as applied at one node. `lat` selects the population set the op

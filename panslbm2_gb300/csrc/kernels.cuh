@@ -113,11 +113,12 @@ __device__ __forceinline__ void node_tail(const KArgs &a, int idx, int code, typ
             T up[3] = {T(0), T(0), T(0)}, kp = T(0);
             if (a.bcu[0]) { up[0] = T(a.bcu[0][idx]); up[1] = T(a.bcu[1][idx]); if (L::ND == 3) up[2] = T(a.bcu[2][idx]); }
             if (a.bckappa) kp = T(a.bckappa[idx]);
-            const uint32_t code8 = rec.code, nops = rec.nops;
+            const uint64_t code16 = rec.code;
+            const uint32_t nops = rec.nops;
             for (int m = 0; m < (int)nops; ++m) {
-                const uint32_t b = (code8 >> (8 * m)) & 0xffu;
-                simple_op<L, T>(int((b >> 3) & 3u), (b & 32u) ? 1 : -1, int(b & 7u), (b & 64u) ? 1 : 0,
-                                (b & 128u) ? 2 : 1, T(rec.v[m]), T(rec.w[m]), f, g, up, kp);
+                const uint32_t b = uint32_t(code16 >> (16 * m)) & 0xffffu;
+                simple_op<L, T>(int((b >> 4) & 3u), (b & 64u) ? 1 : -1, int(b & 15u), (b & 128u) ? 1 : 0,
+                                (b & 256u) ? 2 : 1, rec.val[m], a.uscale, f, g, up, kp);
             }
         }
     }
