@@ -342,9 +342,11 @@ def design_cpu(p, ss, nf, na, budget_s):
                                                                              "rate")}
 
 
-def surrogate_leg(tol=1e-5, seeds=(0, 1, 2)):
-    """config 4: plain vs learned warm start on 160x160x80 FP32, held-out designs (seeds 0, 1, 2;
-    the training designs are seeds 1000 and up)"""
+def surrogate_leg(tol=1e-5, seeds=(0, 1, 2, 3, 4), max_steps=40000, fallback=20000):
+    """config 4: plain vs learned warm start on 160x160x80 FP32, held-out designs (seeds 0-4; the
+    training designs are seeds 1000 and up). Warm starts: "both" seeds the forward and the
+    adjoint problems (a seeded adjoint not converged after `fallback` steps restarts from rest),
+    "forward" seeds the forward problem only."""
     from panslbm2_gb300 import _capi as A
     from panslbm2_gb300 import forced as FC
     from panslbm2_gb300.surrogate import SurrogateWarmStart, default_weights_path
@@ -355,34 +357,39 @@ def surrogate_leg(tol=1e-5, seeds=(0, 1, 2)):
     sw = SurrogateWarmStart(p, "fp32")
     meta = sw.net.load(path)
     sw.iterate(p.design(seed=seeds[0]), True, tol=1e-2, max_steps=300)    # warm-up: programs, taps, kernels
-    out = {"lattice": "forced3d-160x160x80-fp32", "tol": tol, "design_seeds": list(seeds),
+    out = {"lattice": "forced3d-160x160x80-fp32", "tol": tol, "max_steps": max_steps, "fallback_steps": fallback,
+           "design_seeds": list(seeds),
            "training": {k: meta.get(k) for k in ("nsamples", "epochs", "seeds", "data_tol")}, "designs": []}
-    tot = {"plain": [0.0, 0], "surrogate": [0.0, 0]}
+    modes = (("plain", False, None), ("warm_both", True, "both"), ("warm_forward", True, "forward"))
+    tot = {m[0]: [0.0, 0] for m in modes}
     for sd in seeds:
         s = p.design(seed=sd)
         row = {"seed": sd}
-        for name, warm in (("plain", False), ("surrogate", True)):
-            r = sw.iterate(s, warm, tol=tol, max_steps=60000)
+        for name, warm, mode in modes:
+            r = sw.iterate(s, warm, tol=tol, max_steps=max_steps, mode=mode or "both",
+                           adjoint_fallback=fallback if mode == "both" else None)
             row[name] = {"seconds": round(r["seconds"]["total"], 3),
-                         "phases_s": {k: round(v, 3) for k, v in r["seconds"].items()},
                          "forward_steps": r["forward"][1], "adjoint_steps": r["adjoint"][1],
                          "converged": [r["forward"][0] == A.PL_CONVERGED, r["adjoint"][0] == A.PL_CONVERGED],
-                         "objective": r["objective"]}
-        a, b = row["plain"], row["surrogate"]
-        row["objective_rel_diff"] = abs(a["objective"] - b["objective"]) / abs(a["objective"])
-        row["counted"] = all(a["converged"]) and all(b["converged"])
+                         "adjoint_restarted": r["adjoint_restarted"], "objective": r["objective"]}
+        row["counted"] = all(all(row[m[0]]["converged"]) for m in modes)
         if row["counted"]:
             for name in tot:
                 tot[name][0] += row[name]["seconds"]
                 tot[name][1] += row[name]["forward_steps"] + row[name]["adjoint_steps"]
+            row["objective_rel_diff"] = {m: abs(row[m]["objective"] - row["plain"]["objective"]) /
+                                         abs(row["plain"]["objective"]) for m in ("warm_both", "warm_forward")}
         out["designs"].append(row)
     sw.close()
-    if tot["surrogate"][0] > 0:
-        out["speedup"] = round(tot["plain"][0] / tot["surrogate"][0], 3)
-        out["step_ratio"] = round(tot["plain"][1] / tot["surrogate"][1], 3)
+    out["counted_designs"] = sum(1 for r in out["designs"] if r["counted"])
+    if tot["plain"][0] > 0:
+        for m in ("warm_both", "warm_forward"):
+            out["speedup_" + m] = round(tot["plain"][0] / tot[m][0], 3)
+            out["step_ratio_" + m] = round(tot["plain"][1] / tot[m][1], 3)
     out["what"] = ("design iteration (filter, forward, adjoint, sensitivity) from rest vs from the U-Net's predicted "
-                   "fields, both to the same residual tolerance; speedup and step_ratio over the designs whose four "
-                   "solves converged; FP32 residuals on this lattice level off near 4e-6, so the comparison is at 1e-5")
+                   "fields, all to the same residual tolerance; speedups over the designs where every run converged "
+                   "(some designs' adjoint residual levels off near 5e-4 from any start and never converges); FP32 "
+                   "residuals on this lattice level off near 4e-6, so the comparison is at 1e-5")
     return out
 
 
@@ -412,11 +419,13 @@ def precision_leg(nf=4000, na=4000):
     return out
 
 
-def dropin_leg(steps=400):
+def dropin_leg(steps=1000, short=200):
     """The drop-in: a heat-sink driver written against the reference's template API
     (tests/dropin/heatsink_driver.cpp, the calls of production/heatsink3D.cpp's forward loop in
-    the same order, saving every step) built on dropin/src, on the 160x160x80 lattice with FP32
-    storage; its loop time against pl_step's on the same workload"""
+    the same order, saving every step, residual check every 100 steps) built on dropin/src, on
+    the 160x160x80 lattice with FP32 storage; its loop time against pl_step's on the same
+    workload. Until the loop's first residual check the outputs are written back every step;
+    the per-step rate is the difference of a long and a short run, both past that point."""
     import shutil
     import struct
     import tempfile
@@ -438,7 +447,7 @@ def dropin_leg(steps=400):
     fields = [alpha, kappa, dads, dkds, one, zero, zero, zero, zero] + [zero] * 8
     fin, fout = os.path.join(tmp, "in.bin"), os.path.join(tmp, "out.bin")
     res = {}
-    for nsteps in (20, steps):
+    for nsteps in (short, steps):
         with open(fin, "wb") as fh:
             fh.write(struct.pack("6i", 3, p.lx, p.ly, p.lz, nsteps, 1))
             fh.write(struct.pack("7d", p.nu, p.gx, p.gy, p.gz, p.tem0, p.qn, p.L))
@@ -451,7 +460,7 @@ def dropin_leg(steps=400):
                 res[nsteps] = float(line.split()[1])
     shutil.rmtree(tmp, ignore_errors=True)
     # the per-step rate from the difference of a long and a short run (start-up excluded)
-    per_step = (res[steps] - res[20]) / (steps - 20)
+    per_step = (res[steps] - res[short]) / (steps - short)
     # pl_step on the same workload with the same every-step saves, for the ratio
     from panslbm2_gb300 import _capi as A
     from panslbm2_gb300.lattice import LatticePair, phys
@@ -478,7 +487,8 @@ def dropin_leg(steps=400):
             "mlups": round(n / per_step / 1e6, 1), "pl_step_saving_ms": round(api * 1e3, 4),
             "ratio_to_pl_step": round(per_step / api, 3),
             "what": "forward loop of a driver on the template API, collide with saves every step + 2 streams + "
-                    "boundary calls + smoothing, outputs left on the device until the next phase boundary"}
+                    "boundary calls + smoothing + residual every 100 steps; after the first residual the outputs "
+                    "stay on the device until the next phase boundary"}
 
 
 def fp64_leg(steps=200):

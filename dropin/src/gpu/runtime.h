@@ -263,10 +263,14 @@ inline std::map<const void *, Pair *> &saved_arrays() {
 
 //  Host output arrays whose values are still on the device: a saving collide leaves its outputs in
 //  the library's two save slots per family and records here which save each host array stands
-//  for. They are written back when the driver reaches a phase boundary (an initial condition, a
-//  sensitivity, a filter, an export, a population copy: sync_outputs) or just before their save
-//  slot is overwritten (two saves later, when the array is not saved into again). Inside a time
-//  loop nothing is copied to the host: the residual reads the device slots.
+//  for. A family defers only inside a residual-driven loop: from the first Residual that the
+//  library answers from that family's device slots until the next phase boundary. There, outputs
+//  are written back when the driver reaches the boundary (an initial condition, a sensitivity, a
+//  filter, an export, a population copy: sync_outputs) or just before their save slot is
+//  overwritten (two saves later, when the array is not saved into again), and the residual reads
+//  the device slots. Outside such a loop (a driver that reads the outputs on the host every step,
+//  as test/elsens.cpp sums the displacement) every saving collide writes its outputs back.
+//  PANSLBM2_GPU_EAGER_OUTPUTS=1 writes back after every saving collide, always.
 struct Pending {
     const void *key;  // the host array
     Pair *pair;
@@ -309,6 +313,7 @@ struct Pair {
     const void *adj_save[11] = {}, *adj_prev[11] = {};
     bool fwd_saved = false, adj_saved = false;
     long long fwd_gen = 0, adj_gen = 0;   // saves per family
+    bool defer[2] = {false, false};       // forward / adjoint: inside a residual-driven loop
 
     // snapshots: the host array the device slot stands for, and whether the device copy still
     // has to be taken from the last collide
@@ -559,6 +564,8 @@ struct Pair {
                 saved_arrays()[outs[m]] = this;
             }
             (adjoint ? adj_saved : fwd_saved) = true;
+            static const bool eager = env_flag("PANSLBM2_GPU_EAGER_OUTPUTS");
+            if (eager || !defer[slot]) write_back([&](const Pending &e) { return e.adjoint == adjoint; });
         }
         if (saves_snap) {
             snap_owner[slot] = snap;
@@ -593,7 +600,10 @@ struct Pair {
 //  phase boundary: every host output array takes its value from the device, and host inputs are
 //  compared with their uploads again at their next use
 inline void sync_outputs() {
-    for (Pair *p : live_pairs()) p->write_back([](const Pending &) { return true; });
+    for (Pair *p : live_pairs()) {
+        p->write_back([](const Pending &) { return true; });
+        p->defer[0] = p->defer[1] = false;
+    }
     ++input_epoch();
 }
 //  the VTK exporters read host arrays through the driver's functors: sync before they do

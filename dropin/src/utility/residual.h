@@ -18,6 +18,7 @@ namespace PANSLBM2 {
                     pr.flush();
                     double out = 0.0;
                     ck(pl_residual(pr.h, fam, &out), "pl_residual");
+                    pr.defer[fam >= 2 ? 1 : 0] = true;   // a residual-driven loop: later saves stay on the device
                     return T(out);
                 }
             }

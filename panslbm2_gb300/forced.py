@@ -277,10 +277,12 @@ class ForcedHeatSink:
         return ss, (st_f, nf), (st_a, na)
 
     def iterate(self, s, tol=1e-6, max_steps=100000, check_every=100, seed=None, filtered=None,
-                fixed_steps=None):
+                fixed_steps=None, adjoint_fallback=None):
         """One design iteration. `seed` (dict of predicted fields, see FWD_FIELDS / ADJ_FIELDS)
-        replaces the at-rest initial conditions; `fixed_steps` = (nf, na) runs exactly that many
-        forward / adjoint steps instead of the residual loops (parity tests)."""
+        replaces the at-rest initial conditions (a seed without adjoint fields seeds the forward
+        problem only); `fixed_steps` = (nf, na) runs exactly that many forward / adjoint steps
+        instead of the residual loops (parity tests). adjoint_fallback = K: a seeded adjoint that
+        has not converged after K steps is restarted from rest (its steps count in the total)."""
         p, lp, n, t = self.p, self.lp, self.n, {}
         t0 = time.perf_counter()
         ss = self.filtered(s) if filtered is None else p.project(filtered)
@@ -303,9 +305,17 @@ class ForcedHeatSink:
         t2 = time.perf_counter()
         fwd = {k: lp.get_field(f) for k, f in zip(FWD_FIELDS, (A.FWD_RHO, A.FWD_UX, A.FWD_UY, A.FWD_UZ, A.FWD_TEM))}
         fu = (fwd["ux"], fwd["uy"], fwd["uz"])
-        self.seed_adjoint(fu, None if seed is None else seed)
+        adj_seed = seed if seed is not None and any(k in seed for k in ADJ_FIELDS) else None
+        self.seed_adjoint(fu, adj_seed)
+        fallback = False
         if fixed_steps is None:
-            st_a, steps_a, res_a = lp.solve(A.AAD_FORCE, self.ph, self.prog_a, max_steps, check_every, tol)
+            first = max_steps if adj_seed is None or adjoint_fallback is None else min(max_steps, adjoint_fallback)
+            st_a, steps_a, res_a = lp.solve(A.AAD_FORCE, self.ph, self.prog_a, first, check_every, tol)
+            if st_a != A.PL_CONVERGED and first < max_steps:
+                fallback = True
+                self.seed_adjoint(fu, None)
+                st_a, more, res_a = lp.solve(A.AAD_FORCE, self.ph, self.prog_a, max_steps, check_every, tol)
+                steps_a += more
         else:
             steps_a = fixed_steps[1]
             lp.collide(A.AAD_FORCE, self.ph, save=True)
@@ -330,4 +340,5 @@ class ForcedHeatSink:
         t["sensitivity"] = time.perf_counter() - t3
         t["total"] = time.perf_counter() - t0
         return dict(objective=J, ss=ss, dJdss=dJdss, dJds=dJds, fwd=fwd, adj=adj,
-                    forward=(st_f, steps_f, res_f), adjoint=(st_a, steps_a, res_a), seconds=t)
+                    forward=(st_f, steps_f, res_f), adjoint=(st_a, steps_a, res_a), seconds=t,
+                    adjoint_restarted=fallback)

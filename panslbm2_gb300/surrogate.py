@@ -238,16 +238,22 @@ class SurrogateWarmStart:
     def train(self, nsamples, epochs, batch=1, lr=1e-3, seed=0):
         return self.net.train(nsamples, epochs, batch, lr, seed)
 
-    def iterate(self, s, warm, tol=1e-6, max_steps=100000):
-        """one design iteration; warm = True seeds the solver from the network's prediction"""
+    def iterate(self, s, warm, tol=1e-6, max_steps=100000, mode="both", adjoint_fallback=None):
+        """one design iteration; warm = True seeds the solver from the network's prediction:
+        mode "both" seeds the forward and the adjoint problems, "forward" the forward one only
+        (the adjoint then starts from rest); adjoint_fallback: see ForcedHeatSink.iterate"""
         seed = None
         tp = 0.0
         if warm:
             t0 = time.perf_counter()
             ss = self.hs.filtered(s)
             seed = seed_of(self.net.predict(ss))
+            if mode == "forward":
+                from .forced import FWD_FIELDS
+                seed = {k: v for k, v in seed.items() if k in FWD_FIELDS}
             tp = time.perf_counter() - t0
-            r = self.hs.iterate(s, tol=tol, max_steps=max_steps, seed=seed, filtered=ss)
+            r = self.hs.iterate(s, tol=tol, max_steps=max_steps, seed=seed, filtered=ss,
+                                adjoint_fallback=adjoint_fallback)
         else:
             r = self.hs.iterate(s, tol=tol, max_steps=max_steps)
         r["seconds"]["predict"] = tp

@@ -153,11 +153,18 @@ int run3d(const Input &in, bool adj, FILE *out) {
     AD::InitialCondition(pg, A[8].data(), A[5].data(), A[6].data(), A[7].data());
     double *pux = ux.data(), *puy = uy.data(), *puz = uz.data(), *puxp = uxp.data(), *puyp = uyp.data(), *puzp = uzp.data();
     double *pqx = qx.data(), *pqy = qy.data(), *pqz = qz.data(), *pqxp = qxp.data(), *pqyp = qyp.data(), *pqzp = qzp.data();
+    double last_res[2] = {0.0, 0.0};
     const auto t0 = std::chrono::steady_clock::now();
     for (int t = 1; t <= in.tf; ++t) {
         AD::MacroBrinkmanCollideNaturalConvection(pf, rho.data(), pux, puy, puz, A[0].data(), in.nu, pg, tem.data(), pqx, pqy,
                                                   pqz, A[1].data(), in.gx, in.gy, in.gz, tem0, true, gi.data());
         if (t == in.tf) break;
+        if (t % 100 == 0) {
+            // the residual check of production/heatsink3D.cpp's loop, without its early exit (the
+            // step count stays fixed)
+            last_res[0] = Residual(pux, puy, puz, puxp, puyp, puzp, n);
+            last_res[1] = Residual(pqx, pqy, pqz, pqxp, pqyp, pqzp, n);
+        }
         pf.Stream();
         pg.Stream();
         pf.BoundaryCondition([=](int _i, int _j, int _k) { return (_i == 0 || _k == 0) ? 2 : 1; });
@@ -174,8 +181,9 @@ int run3d(const Input &in, bool adj, FILE *out) {
     if (!adj) {
         // the time loop's wall time (its outputs written back by the next call, CopyToHost below)
         const auto pop = populations(pf);
-        std::fprintf(stderr, "loop_seconds %.6f steps %d\n",
-                     std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(), in.tf);
+        std::fprintf(stderr, "loop_seconds %.6f steps %d residuals %.3e %.3e\n",
+                     std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(), in.tf,
+                     last_res[0], last_res[1]);
         put(out, pop.data(), (size_t)15 * n);
         put(out, populations(pg).data(), (size_t)15 * n);
         for (const double *p : std::vector<const double *>{rho.data(), pux, puy, puz, tem.data(), pqx, pqy, pqz})
