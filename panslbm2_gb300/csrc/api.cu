@@ -1324,8 +1324,15 @@ int pl_stream(pl_lattice h, int mode, int prog, int both_sets) {
     int r = build_args(h, adjin ? PL_ANS_BRINKMAN : PL_NS_COLLIDE, nullptr, prog, h->cur, h->cur ^ 1, false, !nopull,
                        h->fwd_latest, a, false);
     if (r) return r;
+    // a staged program streams through the fused step's split (inline ops in the pull kernel,
+    // side chains for the other boundary nodes): the direct set is then the non-inline nodes
+    const bool split = prog >= 0 && a.staged && a.icode && !nopull && both_sets && a.nb > 0;
+    if (split) {
+        const Program &P = h->progs[prog];
+        a.ndir = P.ndir; a.dnode = P.dnode; a.dstart = P.dstart; a.dops = P.dops;
+    }
     h->aux(pl::AUX_STREAM_PROGRAM, a, 0, nullptr, both_sets, inverse ? 1 : -1, nullptr, 0, 0.0, h->st);
-    if ((r = check_launch(h, 1))) return r;
+    if ((r = check_launch(h, split ? 1 + (a.ndir > 0) + (a.ns > 0 ? 2 : 0) : 1))) return r;
     h->cur ^= 1;
     h->last_kind = -1;
     return PL_OK;

@@ -105,6 +105,47 @@ static __global__ void __launch_bounds__(32 * kPostWarps) k_bnd_post(KArgs a, in
     }
 }
 
+// stream-only counterparts of the staged boundary kernels: the same pull, ops and smoothing
+// expressions, then the store of the pre-collision state
+static __global__ void __launch_bounds__(128) k_bnd_direct_stream(KArgs a) {
+    constexpr int Q = PL_LAT::Q;
+    const int s = blockIdx.x * 128 + threadIdx.x;
+    if (s >= a.ndir) return;
+    const int node = a.dnode[s];
+    int i, j, k;
+    coords<PL_LAT>(a.geo, node, i, j, k);
+    TC f[Q], g[Q];
+    const TC sf = TC(a.ph.shift_f), sg = TC(a.ph.shift_g);
+    load_node<PL_LAT, PL_STORE, true>(static_cast<const PL_STORE *>(a.src), a.geo, node, i, j, k, true, a.sgn,
+                                      is_interior<PL_LAT>(a.geo, i, j, k), f, g, sf, sg);
+    for (int o = a.dstart[s]; o < a.dstart[s + 1]; ++o) apply_op<PL_LAT, TC>(a.dops[o], f, g, node, a);
+    store_node<PL_LAT, PL_STORE, true>(static_cast<PL_STORE *>(a.dst), a.geo, node, f, g, sf, sg);
+}
+static __global__ void __launch_bounds__(32 * kPostWarps) k_bnd_post_stream(KArgs a) {
+    constexpr int Q = PL_LAT::Q;
+    __shared__ TC val[kPostWarps][2 * Q];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int t = blockIdx.x * kPostWarps + w;
+    if (t >= a.nt) return;
+    const int idx = a.snode[a.tslot[t]];
+    const TC *tb = static_cast<const TC *>(a.tbuf);
+    if (lane < 2 * Q) {
+        const int lat = lane / Q;
+        const int root = a.troot[2 * t + lat];
+        const long long plane = lane;
+        val[w][lane] = root < 0 ? tb[plane * a.ns + (-root - 1)]
+                                : smooth_eval<TC, kSmoothDepth>(a.sexpr, root, tb, plane, a.ns, a.err);
+    }
+    __syncwarp();
+    if (lane == 0) {
+        TC f[Q], g[Q];
+#pragma unroll
+        for (int c = 0; c < Q; ++c) { f[c] = val[w][c]; g[c] = val[w][Q + c]; }
+        store_node<PL_LAT, PL_STORE, true>(static_cast<PL_STORE *>(a.dst), a.geo, idx, f, g, TC(a.ph.shift_f),
+                                           TC(a.ph.shift_g));
+    }
+}
+
 static dim3 interior_grid(const Geo &g) {
     return dim3((g.nx + 31) / 32, (g.ny + 7) / 8, PL_LAT::ND == 2 ? 1 : g.nz);
 }
@@ -187,7 +228,25 @@ void PL_CAT(aux_, PL_NAME)(int op, const KArgs &a, int which, const double *cons
     const int n = a.geo.n;
     switch (op) {
     case AUX_STREAM_PROGRAM:
-        k_stream_program<PL_LAT, PL_STORE><<<(n + 127) / 128, 128, 0, st>>>(a, has_g, sgn);
+        if (a.staged && a.icode && has_g && a.pull && a.nb > 0) {
+            // the fused step's split without its collide: side chains concurrent with the pull
+            cudaStream_t side = static_cast<cudaStream_t>(a.side), side2 = static_cast<cudaStream_t>(a.side2);
+            cudaEventRecord(static_cast<cudaEvent_t>(a.ev_fork), st);
+            cudaStreamWaitEvent(side, static_cast<cudaEvent_t>(a.ev_fork), 0);
+            cudaStreamWaitEvent(side2, static_cast<cudaEvent_t>(a.ev_fork), 0);
+            if (a.ndir > 0) k_bnd_direct_stream<<<(a.ndir + 127) / 128, 128, 0, side>>>(a);
+            if (a.ns > 0) {
+                k_bnd_pre<<<(a.ns + 127) / 128, 128, 0, side2>>>(a);
+                if (a.nt > 0) k_bnd_post_stream<<<(a.nt + kPostWarps - 1) / kPostWarps, 32 * kPostWarps, 0, side2>>>(a);
+            }
+            k_interior_stream<PL_LAT, PL_STORE><<<interior_grid(a.geo), dim3(32, 8), 0, st>>>(a, sgn);
+            cudaEventRecord(static_cast<cudaEvent_t>(a.ev_join), side);
+            cudaEventRecord(static_cast<cudaEvent_t>(a.ev_join2), side2);
+            cudaStreamWaitEvent(st, static_cast<cudaEvent_t>(a.ev_join), 0);
+            cudaStreamWaitEvent(st, static_cast<cudaEvent_t>(a.ev_join2), 0);
+        } else {
+            k_stream_program<PL_LAT, PL_STORE><<<(n + 127) / 128, 128, 0, st>>>(a, has_g, sgn);
+        }
         break;
     case AUX_INIT:
         k_init<PL_LAT, PL_STORE><<<(n + kBlock - 1) / kBlock, kBlock, 0, st>>>(a, which, in[0], in[1], in[2], in[3],

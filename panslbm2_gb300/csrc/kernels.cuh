@@ -100,6 +100,22 @@ template <class L> __device__ __forceinline__ bool on_face(const Geo &g, int i, 
 // After the pull: the node's inline boundary ops, the collide, the boundary velocity the next
 // step's ops read, and the store. Only the op application diverges; every lane of a warp
 // shares the collide.
+// the node's inline boundary ops (InlineRec `code`), in call order
+template <class L, class T>
+__device__ __forceinline__ void inline_ops(const KArgs &a, int idx, int code, T *f, T *g) {
+    const InlineRec &rec = a.irec[code];
+    T up[3] = {T(0), T(0), T(0)}, kp = T(0);
+    if (a.bcu[0]) { up[0] = T(a.bcu[0][idx]); up[1] = T(a.bcu[1][idx]); if (L::ND == 3) up[2] = T(a.bcu[2][idx]); }
+    if (a.bckappa) kp = T(a.bckappa[idx]);
+    const uint64_t code16 = rec.code;
+    const uint32_t nops = rec.nops;
+    for (int m = 0; m < (int)nops; ++m) {
+        const uint32_t b = uint32_t(code16 >> (16 * m)) & 0xffffu;
+        simple_op<L, T>(int((b >> 4) & 3u), (b & 64u) ? 1 : -1, int(b & 15u), (b & 128u) ? 1 : 0,
+                        (b & 256u) ? 2 : 1, rec.val[m], a.uscale, f, g, up, kp);
+    }
+}
+
 template <class L, class S, int K>
 __device__ __forceinline__ void node_tail(const KArgs &a, int idx, int code, typename Store<S>::T *f,
                                           typename Store<S>::T *g, typename Store<S>::T sf,
@@ -108,19 +124,7 @@ __device__ __forceinline__ void node_tail(const KArgs &a, int idx, int code, typ
     constexpr bool HG = kind_has_g(K);
     constexpr bool INL = kind_inline_bc(K);
     if constexpr (INL) {
-        if (code >= 0) {
-            const InlineRec &rec = a.irec[code];
-            T up[3] = {T(0), T(0), T(0)}, kp = T(0);
-            if (a.bcu[0]) { up[0] = T(a.bcu[0][idx]); up[1] = T(a.bcu[1][idx]); if (L::ND == 3) up[2] = T(a.bcu[2][idx]); }
-            if (a.bckappa) kp = T(a.bckappa[idx]);
-            const uint64_t code16 = rec.code;
-            const uint32_t nops = rec.nops;
-            for (int m = 0; m < (int)nops; ++m) {
-                const uint32_t b = uint32_t(code16 >> (16 * m)) & 0xffffu;
-                simple_op<L, T>(int((b >> 4) & 3u), (b & 64u) ? 1 : -1, int(b & 15u), (b & 128u) ? 1 : 0,
-                                (b & 256u) ? 2 : 1, rec.val[m], a.uscale, f, g, up, kp);
-            }
-        }
+        if (code >= 0) inline_ops<L, T>(a, idx, code, f, g);
     }
     T u[3];
     collide_node<L, T, K>(f, g, idx, a, a.save != 0, a.snap_coll, a.geo.np, (INL && !kind_is_adjoint(K)) ? u : nullptr);
@@ -163,6 +167,30 @@ __global__ void __launch_bounds__(kBlock, 4) k_interior(KArgs a) {
     load_node<L, S, HG>(static_cast<const S *>(a.src), a.geo, idx, i, j, k, PULL, kind_is_adjoint(K) ? 1 : -1,
                         is_interior<L>(a.geo, i, j, k), f, g, sf, sg);
     node_tail<L, S, K>(a, idx, PULL ? code : -1, f, g, sf, sg);
+}
+
+// Stream + boundary program without collide over a staged program (both population sets):
+// the same split as the fused step -- this kernel pulls every node the side kernels do not
+// own and applies its inline ops; the direct and staged-smoothing nodes are stored by
+// k_bnd_direct_stream / k_bnd_post_stream. Same grid as k_interior.
+template <class L, class S>
+__global__ void __launch_bounds__(kBlock, 4) k_interior_stream(KArgs a, int sgn) {
+    using T = typename Store<S>::T;
+    const int nx = a.geo.nx;
+    const int i = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y * 8 + threadIdx.y;
+    if (i >= nx || j >= a.geo.ny) return;
+    const int k = blockIdx.z;
+    const int idx = i + nx * (j + a.geo.ny * k);
+    int code = -1;
+    const bool cand = a.geo.flags ? a.geo.flags[idx] != 0 : on_face<L>(a.geo, i, j, k);
+    if (cand) code = a.icode[idx];
+    if (code == -2) return;
+    T f[L::Q], g[L::Q];
+    const T sf = T(a.ph.shift_f), sg = T(a.ph.shift_g);
+    load_node<L, S, true>(static_cast<const S *>(a.src), a.geo, idx, i, j, k, true, sgn, is_interior<L>(a.geo, i, j, k),
+                          f, g, sf, sg);
+    if (code >= 0) inline_ops<L, T>(a, idx, code, f, g);
+    store_node<L, S, true>(static_cast<S *>(a.dst), a.geo, idx, f, g, sf, sg);
 }
 
 // ---- boundary program replay ----------------------------------------------------------------
