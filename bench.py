@@ -522,19 +522,26 @@ def fp64_leg(steps=200):
     bpn = S.bytes_per_node()
     out = {"lattice": "forced2d-1600x800-fp64", "ms_per_step": round(ms, 4), "bytes_per_node": bpn,
            "hbm_frac": round(S.n * bpn / (ms / 1e3) / 1e9 / peak, 4), "fp64_fma_tflops_probe": round(tf.value, 3)}
-    ops = None
+    ops, instr = None, None
     try:
         with open(os.path.join(ROOT, "profiles", "fp64_step_ops.txt")) as fh:
             for line in fh:
                 k, _, v = line.partition(" ")
                 if k == "flops_per_node":
                     ops = float(v)
+                elif k == "dp_instr_per_node":
+                    instr = float(v)
     except OSError:
         pass
     if ops:
         out["fp64_flops_per_node"] = ops
         out["fp64_frac"] = round(S.n * ops / (ms / 1e3) / 1e12 / tf.value, 4)
-        out["bound"] = "fp64" if out["fp64_frac"] > out["hbm_frac"] else "hbm"
+    if instr:
+        # every DADD, DMUL and DFMA takes one FP64 pipe slot; the probe's FMA rate / 2 is the
+        # pipe's instruction rate
+        out["fp64_dp_instr_per_node"] = instr
+        out["fp64_pipe_frac"] = round(S.n * instr / (ms / 1e3) / (tf.value * 1e12 / 2), 4)
+        out["bound"] = "fp64 pipe" if out["fp64_pipe_frac"] > out["hbm_frac"] else "hbm"
     return out
 
 
