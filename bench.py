@@ -574,6 +574,30 @@ def transient_gpu():
                     "time step, forward states recomputed from device checkpoints; no filter or MMA"}
 
 
+def transient_precision(levels=400, every=50):
+    """The fifth configuration's lattice (192x192x96, forced physics, u(t)) over the first
+    `levels` time levels, FP32 against FP64: objective and sensitivity errors of the transient
+    sweep at configuration size (the full 4000 levels in FP64 would take minutes)."""
+    from panslbm2_gb300 import forced as FC
+    from panslbm2_gb300.transient import TransientHeatSink
+    d = TRANSIENT_LATTICE
+    p = FC.ForcedParams(d["nd"], d["lx"], d["ly"], d["lz"])
+    ss = p.project(p.design(seed=0))
+    res = {}
+    for st in ("fp64", "fp32"):
+        tr = TransientHeatSink(p, st, checkpoint_every=every, tau_in=500.0)
+        t0 = time.perf_counter()
+        res[st] = tr.evaluate_design(ss, levels)
+        res[st]["sec"] = time.perf_counter() - t0
+        tr.close()
+    a, b = res["fp32"], res["fp64"]
+    return {"lattice": "forced3d-192x192x96", "time_levels": levels, "checkpoint_every": every,
+            "fp64_objective": b["objective"], "fp64_seconds": round(b["sec"], 3), "fp32_seconds": round(a["sec"], 3),
+            "objective_rel_err": abs(a["objective"] - b["objective"]) / abs(b["objective"]),
+            "sensitivity_rel_err_l2": float(np.linalg.norm(a["dfdss"] - b["dfdss"]) / np.linalg.norm(b["dfdss"])),
+            "sensitivity_rel_err_max": float(np.max(np.abs(a["dfdss"] - b["dfdss"])) / np.max(np.abs(b["dfdss"])))}
+
+
 def run_reference(args, wl):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -707,6 +731,7 @@ def main():
         leg(line, "dropin", dropin_leg)
     if rank == 0 and not args.no_transient:
         leg(line, "transient_iter", transient_gpu)
+        leg(line, "transient_precision", transient_precision)
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_port(S)
     if rank == 0:
