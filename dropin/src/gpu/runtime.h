@@ -773,15 +773,24 @@ void face_values(const Pair &pr, const Fv &qnbc, const Ff &bctype, std::vector<d
 //  weight functor of global coordinates (i1, j1, k1, i2, j2, k2) and verify the functor against
 //  it on every tap inside the lattice. Returns an empty vector for "hat everywhere"; aborts if
 //  the functor has another form. Cached per functor type, captured state and radius.
+struct FilterPlan {
+    std::vector<int> mask;        // hat weight between mask cells (empty: everywhere)
+    bool general = false;         // the functor is not of that form: use `table`
+    std::vector<double> table;    // [node][tap] functor values (pl_filter_taps order)
+};
+//  The drivers' weight functors are the hat weight (R - distance) / R, everywhere or between two
+//  cells of a design region with the identity elsewhere: that region is inferred and checked
+//  on every tap, and the device builds the weights itself. Any other functor is evaluated on
+//  every (node, tap) pair into a table for pl_filter_weighted.
 template <class F>
-const std::vector<int> &filter_mask(const Pair &pr, double R, const F &w) {
-    static std::map<std::string, std::shared_ptr<std::vector<int>>> cache;
+std::shared_ptr<const FilterPlan> filter_plan(const Pair &pr, double R, const F &w) {
+    static std::map<std::string, std::shared_ptr<const FilterPlan>> cache;
     std::string key;
     if (cacheable<F>()) {
         key = functor_key(w, "filter", pr.nx, pr.ny, pr.nz);
         key.append(reinterpret_cast<const char *>(&R), sizeof R);
         auto it = cache.find(key);
-        if (it != cache.end()) return *it->second;
+        if (it != cache.end()) return it->second;
     }
     const int nR = (int)R;
     struct Tap { int a, b, c; double hat; };
@@ -794,6 +803,7 @@ const std::vector<int> &filter_mask(const Pair &pr, double R, const F &w) {
             }
     auto inside = [&](int i, int j, int k) { return 0 <= i && i < pr.nx && 0 <= j && j < pr.ny && 0 <= k && k < pr.nz; };
     auto idx = [&](int i, int j, int k) { return i + (size_t)pr.nx * (j + (size_t)pr.ny * k); };
+    auto plan = std::make_shared<FilterPlan>();
     std::vector<int> m(pr.n, 0);
     for (int k = 0; k < pr.nz; ++k)
         for (int j = 0; j < pr.ny; ++j)
@@ -803,10 +813,10 @@ const std::vector<int> &filter_mask(const Pair &pr, double R, const F &w) {
                     if (!inside(i + t.a, j + t.b, k + t.c)) continue;
                     if (double(w(i, j, k, i + t.a, j + t.b, k + t.c)) != 0.0) { m[idx(i, j, k)] = 1; break; }
                 }
-    bool all = true;
-    for (int k = 0; k < pr.nz; ++k)
-        for (int j = 0; j < pr.ny; ++j)
-            for (int i = 0; i < pr.nx; ++i) {
+    bool all = true, hat = true;
+    for (int k = 0; k < pr.nz && hat; ++k)
+        for (int j = 0; j < pr.ny && hat; ++j)
+            for (int i = 0; i < pr.nx && hat; ++i) {
                 const int mi = m[idx(i, j, k)];
                 all = all && mi;
                 for (const Tap &t : taps) {
@@ -814,16 +824,25 @@ const std::vector<int> &filter_mask(const Pair &pr, double R, const F &w) {
                     if (!inside(i2, j2, k2)) continue;
                     const bool center = t.a == 0 && t.b == 0 && t.c == 0;
                     const double expect = (mi && m[idx(i2, j2, k2)]) ? t.hat : (center ? 1.0 : 0.0);
-                    if (double(w(i, j, k, i2, j2, k2)) != expect)
-                        die("filter weight is not the hat weight (R - distance) / R on a masked region (identity elsewhere)");
+                    if (double(w(i, j, k, i2, j2, k2)) != expect) { hat = false; break; }
                 }
             }
-    auto out = std::make_shared<std::vector<int>>();
-    if (!all) out->swap(m);
-    if (!key.empty()) cache[key] = out;
-    static std::vector<std::shared_ptr<std::vector<int>>> keep;   // uncached results stay alive
-    if (key.empty()) keep.push_back(out);
-    return *out;
+    if (hat) {
+        if (!all) plan->mask.swap(m);
+    } else {
+        const size_t nt = taps.size();
+        plan->general = true;
+        plan->table.assign((size_t)pr.n * nt, 0.0);
+        for (int k = 0; k < pr.nz; ++k)
+            for (int j = 0; j < pr.ny; ++j)
+                for (int i = 0; i < pr.nx; ++i)
+                    for (size_t t = 0; t < nt; ++t) {
+                        const int i2 = i + taps[t].a, j2 = j + taps[t].b, k2 = k + taps[t].c;
+                        if (inside(i2, j2, k2)) plan->table[idx(i, j, k) * nt + t] = double(w(i, j, k, i2, j2, k2));
+                    }
+    }
+    if (!key.empty()) cache[key] = plan;
+    return plan;
 }
 
 template <class T>

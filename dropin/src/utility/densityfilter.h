@@ -11,10 +11,14 @@ namespace PANSLBM2 {
         std::vector<T> GetFilteredValue(P<T>& _p, T _R, const std::vector<T> &_v, F _weight) {
             gpu::Pair &pr = *_p.gpu_particle().pair;
             gpu::sync_outputs();
-            const std::vector<int> &mask = gpu::filter_mask(pr, double(_R), _weight);
+            const auto plan = gpu::filter_plan(pr, double(_R), _weight);
             std::vector<double> v(_v.begin(), _v.end()), out(pr.n);
-            gpu::ck(pl_density_filter(pr.h, double(_R), v.data(), mask.empty() ? nullptr : mask.data(), out.data()),
-                    "pl_density_filter");
+            if (plan->general)
+                gpu::ck(pl_filter_weighted(pr.h, 2, double(_R), 0.0, v.data(), nullptr, plan->table.data(), out.data()),
+                        "pl_filter_weighted");
+            else
+                gpu::ck(pl_density_filter(pr.h, double(_R), v.data(), plan->mask.empty() ? nullptr : plan->mask.data(),
+                                          out.data()), "pl_density_filter");
             return std::vector<T>(out.begin(), out.end());
         }
 

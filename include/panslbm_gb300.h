@@ -323,6 +323,17 @@ int pl_heaviside_var(pl_lattice h, double R, double beta, const double *s, const
 int pl_heaviside_sens(pl_lattice h, double R, double beta, const double *s, const double *dfdrho, const int *mask,
                       double *out);
 int pl_density_filter(pl_lattice h, double R, const double *v, const int *mask, double *out);
+/* the filters with a general weight functor (the `_weight(i1, j1, k1, i2, j2, k2)` argument of
+ * HeavisideFilter::GetFilteredVariable / GetFilteredSensitivity, heavisidefilter.h:404-899, and
+ * DensityFilter::GetFilteredValue, densityfilter.h:10-515). pl_filter_taps lists the taps of
+ * radius R (offsets with distance <= R) in the reference's (i2, j2, k2) loop order: *ntap, and
+ * di/dj/dk when non-NULL (room for (2 floor(R) + 1)^d entries). weights[node * ntap + t] is the
+ * functor's value for node and node + tap t (taps outside the lattice are skipped, as there).
+ * op 0: Heaviside projection of the filtered s (a = s, beta); 1: Heaviside sensitivity (a = s,
+ * b = dfdrho); 2: filtered average of a (DensityFilter). */
+int pl_filter_taps(pl_lattice h, double R, int *ntap, int *di, int *dj, int *dk);
+int pl_filter_weighted(pl_lattice h, int op, double R, double beta, const double *a, const double *b,
+                       const double *weights, double *out);
 /* Normalize (normalize.h:8-23), in place on a host array of n */
 int pl_normalize(pl_lattice h, double *v, int n);
 

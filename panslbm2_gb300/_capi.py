@@ -63,7 +63,7 @@ EXPORTS = [
     "pl_solve", "pl_snapshot", "pl_set_snapshot", "pl_residual", "pl_residual_host", "pl_residual_device_noalloc",
     "pl_sensitivity", "pl_sensitivity_compliance", "pl_store", "pl_load", "pl_store_release", "pl_store_swap_snapshot",
     "pl_sensitivity_device", "pl_accumulate", "pl_heaviside_var",
-    "pl_heaviside_sens", "pl_density_filter", "pl_normalize", "pl_stats", "pl_mma_create", "pl_mma_set_param",
+    "pl_heaviside_sens", "pl_density_filter", "pl_filter_taps", "pl_filter_weighted", "pl_normalize", "pl_stats", "pl_mma_create", "pl_mma_set_param",
     "pl_mma_update", "pl_mma_destroy", "pl_mma_get_state", "pl_mma_set_state", "pl_debug_fail_alloc",
     "pl_unet_create", "pl_unet_destroy", "pl_unet_param_count", "pl_unet_init_params", "pl_unet_get_params",
     "pl_unet_set_params", "pl_unet_forward", "pl_unet_backward", "pl_unet_gradients", "pl_unet_dataset_reserve",

@@ -139,6 +139,8 @@ struct pl_lattice_s {
     std::vector<void *> store[3];
     std::vector<char> snap_filled;   // PL_STORE_SNAP slots that hold a snapshot
     int *sens_mask = nullptr;        // source mask of pl_sensitivity_device
+    double *wtab = nullptr;          // per-(node, tap) filter weights of pl_filter_weighted
+    size_t wtab_len = 0;
     double uscale = 1.0;             // pl_set_inflow_scale
     bool sr = false;                 // PL_OPT_STOCHASTIC_ROUNDING
     uint32_t sr_count = 0;           // launches so far (seeds the stochastic rounding)
@@ -939,6 +941,7 @@ int pl_destroy(pl_lattice h) {
     cudaFree(h->iscratch); cudaFree(h->partial); cudaFree(h->nonfinite); cudaFree(h->err); cudaFree(h->dout);
     for (auto &v : h->store) for (void *p : v) cudaFree(p);
     cudaFree(h->sens_mask);
+    cudaFree(h->wtab);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
     if (h->side) { cudaStreamSynchronize(h->side); cudaStreamDestroy(h->side); }
@@ -1695,7 +1698,7 @@ int pl_accumulate(pl_lattice h, int dst, int src, double a) {
 }
 
 static int filter_common(pl_lattice h, int op, double R, double beta, const double *s, const double *d,
-                         const int *mask, double *out) {
+                         const int *mask, double *out, const double *wtab = nullptr) {
     if (!h || !s || !out || !(R > 0.0) || (op == 1 && !d)) return fail(PL_ERR_ARG, "bad arguments");
     Taps *t = get_taps(h, R);
     if (!t) return fail(PL_ERR_ALLOC, "filter taps");
@@ -1707,9 +1710,21 @@ static int filter_common(pl_lattice h, int op, double R, double beta, const doub
     if ((r = upload(h, ds, s, h->n))) return r;
     if (d && (r = upload(h, dd, d, h->n))) return r;
     if (mask) CK(cudaMemcpyAsync(dm, mask, sizeof(int) * h->n, cudaMemcpyHostToDevice, h->st));
+    if (wtab) {
+        const size_t len = (size_t)h->n * t->ntap;
+        if (h->wtab_len < len) {
+            cudaFree(h->wtab);
+            h->wtab = nullptr;
+            h->wtab_len = 0;
+            if ((r = dalloc((void **)&h->wtab, sizeof(double) * len))) return r;
+            h->wtab_len = len;
+        }
+        if ((r = upload(h, h->wtab, wtab, len))) return r;
+    }
     pl::FiltArgs f;
     f.n = h->n; f.nx = h->nx; f.ny = h->ny; f.nz = h->nz; f.ntap = t->ntap;
     f.di = t->di; f.dj = t->dj; f.dk = t->dk; f.hat = t->hat; f.mask = mask ? dm : nullptr; f.beta = beta;
+    f.wtab = wtab ? h->wtab : nullptr;
     pl::launch_filter(op, f, ds, dd, tmp, dout, h->st);
     if ((r = check_launch(h, op == 1 ? 2 : 1))) return r;
     return download(h, out, dout, h->n);
@@ -1727,6 +1742,31 @@ int pl_heaviside_sens(pl_lattice h, double R, double beta, const double *s, cons
 int pl_density_filter(pl_lattice h, double R, const double *v, const int *mask, double *out) {
     PL_RANGE("pl_density_filter");
     return filter_common(h, 2, R, 0.0, v, nullptr, mask, out);
+}
+
+int pl_filter_taps(pl_lattice h, double R, int *ntap, int *di, int *dj, int *dk) {
+    if (!h || !ntap || !(R > 0.0)) return fail(PL_ERR_ARG, "bad arguments");
+    const int nR = (int)R;
+    int m = 0;
+    for (int a = -nR; a <= nR; ++a)
+        for (int b = -nR; b <= nR; ++b)
+            for (int c = -nR; c <= nR; ++c) {
+                const double dist = std::sqrt(std::pow((double)a, 2.0) + std::pow((double)b, 2.0) + std::pow((double)c, 2.0));
+                if (dist > R || (h->nd == 2 && c != 0)) continue;
+                if (di) di[m] = a;
+                if (dj) dj[m] = b;
+                if (dk) dk[m] = c;
+                ++m;
+            }
+    *ntap = m;
+    return PL_OK;
+}
+
+int pl_filter_weighted(pl_lattice h, int op, double R, double beta, const double *a, const double *b,
+                       const double *weights, double *out) {
+    PL_RANGE("pl_filter_weighted");
+    if (!h || op < 0 || op > 2 || !weights) return fail(PL_ERR_ARG, "bad arguments");
+    return filter_common(h, op, R, beta, a, op == 1 ? b : nullptr, nullptr, out, weights);
 }
 
 int pl_normalize(pl_lattice h, double *v, int n) {

@@ -209,7 +209,8 @@ void launch_axpy(int n, double *dst, const double *src, double a, cudaStream_t s
 
 // ---- filters ------------------------------------------------------------------------------
 // Taps of the (2 nR + 1)^d box with distance <= R, in the reference's (i2, j2, k2) loop order,
-// with their hat weights (R - dist)/R computed on the host in FP64.
+// with their hat weights (R - dist)/R computed on the host in FP64; or, for a general weight
+// functor, one weight per (node, tap) from the caller's table.
 __device__ __forceinline__ void filt_node(const FiltArgs &f, const double *v, int idx, double &ws, double &w) {
     const int i = idx % f.nx, r = idx / f.nx, j = r % f.ny, k = r / f.ny;
     const bool m1 = f.mask ? f.mask[idx] != 0 : true;
@@ -220,7 +221,8 @@ __device__ __forceinline__ void filt_node(const FiltArgs &f, const double *v, in
         if (i2 < 0 || i2 >= f.nx || j2 < 0 || j2 >= f.ny || k2 < 0 || k2 >= f.nz) continue;
         const int id2 = i2 + f.nx * (j2 + f.ny * k2);
         double wt;
-        if (!f.mask || (m1 && f.mask[id2])) wt = f.hat[t];
+        if (f.wtab) wt = f.wtab[(long long)idx * f.ntap + t];
+        else if (!f.mask || (m1 && f.mask[id2])) wt = f.hat[t];
         else wt = (f.di[t] == 0 && f.dj[t] == 0 && f.dk[t] == 0) ? 1.0 : 0.0;
         ws += wt * v[id2];
         w += wt;

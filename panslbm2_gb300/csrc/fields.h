@@ -39,6 +39,7 @@ struct FiltArgs {
     const double *hat;
     const int *mask;
     double beta;
+    const double *wtab;   // [n][ntap] weights of a general weight functor; replaces hat and mask
 };
 // op 0: Heaviside projection of the filtered value; 1: Heaviside sensitivity (two passes,
 // tmp = N doubles); 2: plain filtered average (DensityFilter)

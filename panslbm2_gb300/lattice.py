@@ -266,6 +266,29 @@ class LatticePair:
                                          None if mask is None else mask.ctypes.data_as(A.IPT), _dp(out)))
         return out
 
+    def filter_taps(self, R):
+        """(di, dj, dk) of the filter taps of radius R in the reference's loop order"""
+        nR = int(R)
+        cap = (2 * nR + 1) ** 3
+        n = C.c_int()
+        di, dj, dk = (np.zeros(cap, np.int32) for _ in range(3))
+        ip = lambda a: a.ctypes.data_as(A.IPT)  # noqa: E731
+        check(self.lib.pl_filter_taps(self.h, C.c_double(R), C.byref(n), ip(di), ip(dj), ip(dk)))
+        return di[:n.value].copy(), dj[:n.value].copy(), dk[:n.value].copy()
+
+    def filter_weighted(self, op, R, a, weights, b=None, beta=0.0):
+        """filters with a general weight table weights[node, tap] (op 0: Heaviside variable,
+        1: Heaviside sensitivity with b = dfdrho, 2: density filter)"""
+        a, out = _f64(a, self.n), np.empty(self.n)
+        b = _f64(b, self.n) if b is not None else None
+        w = np.ascontiguousarray(weights, np.float64)
+        ntap = len(self.filter_taps(R)[0])
+        if w.size != self.n * ntap:
+            raise ValueError("expected %d x %d weights, got %d" % (self.n, ntap, w.size))
+        check(self.lib.pl_filter_weighted(self.h, op, C.c_double(R), C.c_double(beta), _dp(a),
+                                          None if b is None else _dp(b), _dp(w), _dp(out)))
+        return out
+
     def normalize(self, v):
         v = _f64(v).copy()
         check(self.lib.pl_normalize(self.h, _dp(v), v.size))

@@ -30,7 +30,7 @@ def _compile(src, out, extra=()):
     assert p.returncode == 0, p.stderr[-4000:]
 
 
-@pytest.mark.parametrize("driver", ["heatsink_driver", "nsin_channel_driver", "elastic_driver"])
+@pytest.mark.parametrize("driver", ["heatsink_driver", "nsin_channel_driver", "elastic_driver", "filter_driver"])
 def test_test_driver_builds(tmp_path, driver):
     _compile(os.path.join(ROOT, "tests", "dropin", driver + ".cpp"), str(tmp_path / driver))
 
