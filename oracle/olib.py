@@ -86,6 +86,7 @@ class Oracle:
         L = self.lib
         L.ol_residual.restype = C.c_double
         L.ol_nnodes.restype = C.c_int
+        L.ol_filter_ntaps.restype = C.c_int
 
     def set_threads(self, n):
         self.lib.ol_set_threads(int(n))
@@ -151,6 +152,20 @@ class Oracle:
     def density_filter(self, L, R, v, mask=None):
         out = np.zeros_like(v)
         self.lib.ol_density_filter(C.byref(L), C.c_double(R), _dp(v), _ip(mask), _dp(out))
+        return out
+
+    def filter_ntaps(self, L, R):
+        return int(self.lib.ol_filter_ntaps(C.byref(L), C.c_double(R)))
+
+    def filter_table(self, L, op, R, a, w, b=None, beta=0.0):
+        """the filters with a weight table w[node][tap] (op 0 / 1 / 2: Heaviside variable,
+        Heaviside sensitivity with b = dfdrho, density filter)"""
+        a = np.ascontiguousarray(a, np.float64)
+        w = np.ascontiguousarray(w, np.float64)
+        out = np.zeros_like(a)
+        bb = None if b is None else np.ascontiguousarray(b, np.float64)
+        self.lib.ol_filter_table(C.byref(L), op, C.c_double(R), C.c_double(beta), _dp(a), None if bb is None else _dp(bb),
+                                 _dp(w), _dp(out))
         return out
 
     def residual(self, a, b):

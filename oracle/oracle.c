@@ -1258,6 +1258,63 @@ void ol_density_filter(const ol_lat *L, double R, const double *v, const int *ma
             }
 }
 
+/* Filters with a general weight functor (heavisidefilter.h:452-475, 770-800; densityfilter.h):
+ * the functor's values come as a table w[node][tap], the taps being the offsets with distance
+ * <= R in the (i2, j2, k2) loop order (2D: k2 = k1 only); out-of-lattice taps are skipped. */
+static int ntaps(const lat_t *t, double R) {
+    int nR = (int)R, m = 0;
+    for (int a = -nR; a <= nR; ++a)
+        for (int b = -nR; b <= nR; ++b)
+            for (int c = (t->nd == 3 ? -nR : 0); c <= (t->nd == 3 ? nR : 0); ++c)
+                if (sqrt(pow((double)a, 2.0) + pow((double)b, 2.0) + pow((double)c, 2.0)) <= R) ++m;
+    return m;
+}
+static wsum_t filt_tab(const lat_t *t, double R, const double *v, const double *w, int ntap, int i1, int j1, int k1) {
+    int nR = (int)R, tap = 0;
+    size_t row = (size_t)IDX(t, i1, j1, k1) * (size_t)ntap;
+    wsum_t r = {0.0, 0.0};
+    for (int i2 = i1 - nR; i2 <= i1 + nR; ++i2)
+        for (int j2 = j1 - nR; j2 <= j1 + nR; ++j2)
+            for (int k2 = (t->nd == 3 ? k1 - nR : k1); k2 <= (t->nd == 3 ? k1 + nR : k1); ++k2) {
+                double dist = sqrt(pow(i1 - i2, 2.0) + pow(j1 - j2, 2.0) + pow(k1 - k2, 2.0));
+                if (dist > R) continue;
+                int tp = tap++;
+                if (i2 < 0 || i2 >= t->nx || j2 < 0 || j2 >= t->ny || k2 < 0 || k2 >= t->nz) continue;
+                double wt = w[row + tp];
+                r.ws += wt * v[i2 + t->nx * (j2 + t->ny * k2)];
+                r.w += wt;
+            }
+    return r;
+}
+int ol_filter_ntaps(const ol_lat *L, double R) { lat_t T = mk(L); return ntaps(&T, R); }
+void ol_filter_table(const ol_lat *L, int op, double R, double beta, const double *a, const double *b,
+                     const double *w, double *out) {
+    lat_t T = mk(L); const lat_t *t = &T;
+    int nt = ntaps(t, R);
+    double *tmp = NULL;
+    if (op == 1) tmp = (double *)malloc(sizeof(double) * (size_t)t->n);
+#pragma omp parallel for collapse(2)
+    for (int k = 0; k < t->nz; ++k)
+        for (int j = 0; j < t->ny; ++j)
+            for (int i = 0; i < t->nx; ++i) {
+                wsum_t r = filt_tab(t, R, a, w, nt, i, j, k);
+                int idx = IDX(t, i, j, k);
+                if (op == 0) out[idx] = 0.5 * (tanh(0.5 * beta) + tanh(beta * (r.ws / r.w - 0.5))) / tanh(0.5 * beta);
+                else if (op == 1) tmp[idx] = b[idx] * (0.5 * beta * (1.0 - pow(tanh(beta * (r.ws / r.w - 0.5)), 2.0)) / tanh(0.5 * beta));
+                else out[idx] = r.ws / r.w;
+            }
+    if (op == 1) {
+#pragma omp parallel for collapse(2)
+        for (int k = 0; k < t->nz; ++k)
+            for (int j = 0; j < t->ny; ++j)
+                for (int i = 0; i < t->nx; ++i) {
+                    wsum_t r = filt_tab(t, R, tmp, w, nt, i, j, k);
+                    out[IDX(t, i, j, k)] = r.ws / r.w;
+                }
+        free(tmp);
+    }
+}
+
 /* ---- Residual (residual.h:8-51) / Normalize (normalize.h:8-23) ------------------------- */
 double ol_residual(int n, int ncomp, const double *const *a, const double *const *b) {
     double s0 = 0.0, s1 = 0.0;

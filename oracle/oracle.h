@@ -160,6 +160,12 @@ void ol_heaviside_var(const ol_lat *L, double R, double beta, const double *s, c
 void ol_heaviside_sens(const ol_lat *L, double R, double beta, const double *s, const double *dfdrho,
                        const int *mask, double *out);
 void ol_density_filter(const ol_lat *L, double R, const double *v, const int *mask, double *out);
+/* the same filters with a general weight functor given as a table w[node][tap] (taps: offsets
+ * with distance <= R in the (i2, j2, k2) loop order; 2D: k2 = k1). op 0: Heaviside variable of
+ * a (beta); 1: Heaviside sensitivity (a = s, b = dfdrho); 2: filtered average of a. */
+int ol_filter_ntaps(const ol_lat *L, double R);
+void ol_filter_table(const ol_lat *L, int op, double R, double beta, const double *a, const double *b,
+                     const double *w, double *out);
 
 /* Residual (residual.h) over ncomp components, Normalize (normalize.h). */
 double ol_residual(int n, int ncomp, const double *const *a, const double *const *b);

@@ -1,6 +1,7 @@
 // ref_api.cpp -- exports the oracle API names from the reference-backed library, dispatching on
 // the lattice (q = 9 -> D2Q9 translation unit, q = 15 -> D3Q15 translation unit). TEST ONLY.
 #include "oracle.h"
+#include <cmath>
 #ifdef _OPENMP
 #include <omp.h>
 #endif
@@ -16,7 +17,8 @@
     extern "C" void ref##dim##_sensitivity(const ol_lat *, int, double *, const ol_fields *, const double *, const double *, const double *, const double *, const double *, const int *); \
     extern "C" void ref##dim##_heaviside_var(const ol_lat *, double, double, const double *, const int *, double *); \
     extern "C" void ref##dim##_heaviside_sens(const ol_lat *, double, double, const double *, const double *, const int *, double *); \
-    extern "C" void ref##dim##_density_filter(const ol_lat *, double, const double *, const int *, double *);
+    extern "C" void ref##dim##_density_filter(const ol_lat *, double, const double *, const int *, double *); \
+    extern "C" void ref##dim##_filter_table(const ol_lat *, int, double, double, const double *, const double *, const double *, double *);
 DECL(2)
 DECL(3)
 extern "C" double ref_residual(int, int, const double *const *, const double *const *);
@@ -47,6 +49,19 @@ void ol_sensitivity(const ol_lat *L, int which, double *dfds, const ol_fields *F
 void ol_heaviside_var(const ol_lat *L, double R, double beta, const double *s, const int *mask, double *out) { DISPATCH(heaviside_var, L, R, beta, s, mask, out); }
 void ol_heaviside_sens(const ol_lat *L, double R, double beta, const double *s, const double *d, const int *mask, double *out) { DISPATCH(heaviside_sens, L, R, beta, s, d, mask, out); }
 void ol_density_filter(const ol_lat *L, double R, const double *v, const int *mask, double *out) { DISPATCH(density_filter, L, R, v, mask, out); }
+int ol_filter_ntaps(const ol_lat *L, double R) {
+    const int nR = (int)R, three = L->q != 9;
+    int m = 0;
+    for (int a = -nR; a <= nR; ++a)
+        for (int b = -nR; b <= nR; ++b)
+            for (int c = (three ? -nR : 0); c <= (three ? nR : 0); ++c)
+                if (std::sqrt(std::pow((double)a, 2.0) + std::pow((double)b, 2.0) + std::pow((double)c, 2.0)) <= R) ++m;
+    return m;
+}
+void ol_filter_table(const ol_lat *L, int op, double R, double beta, const double *a, const double *b, const double *w,
+                     double *out) {
+    DISPATCH(filter_table, L, op, R, beta, a, b, w, out);
+}
 double ol_residual(int n, int ncomp, const double *const *a, const double *const *b) { return ref_residual(n, ncomp, a, b); }
 void ol_normalize(double *v, int n) { ref_normalize(v, n); }
 }

@@ -294,6 +294,34 @@ extern "C" void NAME(density_filter)(const ol_lat *L, double R, const double *v,
     delete p;
 }
 
+/* the filters with a general weight functor: the reference's own routines called with a functor
+ * that reads the table w[node][tap] (taps: offsets within R in the (i2, j2, k2) loop order; 2D:
+ * k2 = k1 only, the other offsets are never inside the lattice) */
+extern "C" void NAME(filter_table)(const ol_lat *L, int op, double R, double beta, const double *a, const double *b,
+                                   const double *w, double *out) {
+    Lat *p = make(L);
+    const int nR = (int)R, span = 2 * nR + 1;
+    std::vector<int> tapix((size_t)span * span * span, -1);
+    int nt = 0;
+    for (int da = -nR; da <= nR; ++da)
+        for (int db = -nR; db <= nR; ++db)
+            for (int dc = (REF_DIM == 3 ? -nR : 0); dc <= (REF_DIM == 3 ? nR : 0); ++dc)
+                if (sqrt(pow((double)da, 2.0) + pow((double)db, 2.0) + pow((double)dc, 2.0)) <= R)
+                    tapix[((size_t)(da + nR) * span + (db + nR)) * span + (dc + nR)] = nt++;
+    const int nx = L->nx, ny = L->ny;
+    auto weight = [&](int i1, int j1, int k1, int i2, int j2, int k2) {
+        const int t = tapix[((size_t)(i2 - i1 + nR) * span + (j2 - j1 + nR)) * span + (k2 - k1 + nR)];
+        if (t < 0) return 0.0;
+        return w[((size_t)i1 + (size_t)nx * ((size_t)j1 + (size_t)ny * k1)) * nt + t];
+    };
+    std::vector<double> av(a, a + p->nxyz), r;
+    if (op == 0) r = HeavisideFilter::GetFilteredVariable(*p, R, beta, av, weight);
+    else if (op == 1) r = HeavisideFilter::GetFilteredSensitivity(*p, R, beta, av, std::vector<double>(b, b + p->nxyz), weight);
+    else r = DensityFilter::GetFilteredValue(*p, R, av, weight);
+    std::memcpy(out, r.data(), sizeof(double) * p->nxyz);
+    delete p;
+}
+
 #if REF_DIM == 2
 extern "C" double ref_residual(int n, int ncomp, const double *const *a, const double *const *b) {
     if (ncomp == 1) return Residual(a[0], b[0], n);

@@ -229,6 +229,24 @@ def test_filters(libs, shape, R, masked):
     _eq(o.density_filter(L, R, s, mask), r.density_filter(L, R, s, mask))
 
 
+@pytest.mark.parametrize("shape", [(9, 13, 11, 1), (15, 7, 8, 6)])
+@pytest.mark.parametrize("R", [1.5, 2.4, 3.0])
+def test_filters_general_weight(libs, shape, R):
+    """a weight functor of no special form (here a random positive table per node and tap):
+    the oracle's table restatement equals the reference's routines called with that functor"""
+    o, r = libs
+    q, nx, ny, nz = shape
+    L = o.lat(q, nx, ny, nz)
+    n = L.nx * L.ny * L.nz
+    nt = o.filter_ntaps(L, R)
+    assert nt == r.filter_ntaps(L, R)
+    rng = np.random.default_rng(17)
+    s, dfd = field(rng, n, 0, 1), field(rng, n, -1, 1)
+    w = 0.1 + rng.random((n, nt))
+    for op in (0, 1, 2):
+        _eq(o.filter_table(L, op, R, s, w, b=dfd, beta=8.0), r.filter_table(L, op, R, s, w, b=dfd, beta=8.0))
+
+
 @pytest.mark.parametrize("ncomp", [1, 2, 3])
 def test_residual_normalize(libs, ncomp):
     o, r = libs
