@@ -1,7 +1,11 @@
 // inst_body.cuh -- explicit kernel instantiations and launch switch for one
-// (lattice, storage) pair. Included by inst_<lattice>_<storage>.cu with PL_LAT, PL_STORE and
-// PL_NAME defined; PL_ALL_KINDS selects every collide kind (else the primary ones only) and
-// PL_INCOMPRESSIBLE adds the D2Q9-only NSin / ANSin kinds, PL_ELASTIC the D2Q9-only EL / AEL kinds.
+// (lattice, storage) pair. Included by inst_<lattice>_<storage>{,_adj,_misc,_aux,_side}.cu with PL_LAT,
+// PL_STORE and PL_NAME defined; PL_ALL_KINDS selects every collide kind (else the primary ones
+// only) and PL_INCOMPRESSIBLE adds the D2Q9-only NSin / ANSin kinds, PL_ELASTIC the D2Q9-only
+// EL / AEL kinds. PL_PART splits one pair over five translation units compiled in parallel
+// (each kernel is the same code in any split): 1, 4, 5 the collide / step launches of the kind
+// groups A, B, C, 2 the auxiliary launches (standalone stream, init, host transfer), 3 the
+// side-stream boundary kernels.
 #include "kernels.cuh"
 #include "launch.h"
 
@@ -11,6 +15,25 @@ namespace pl {
 #define PL_CAT(a, b) PL_CAT2(a, b)
 
 using TC = Store<PL_STORE>::T;
+
+// step launches by kind group: A the forward inline-boundary kinds (and the launch switch),
+// B the adjoint inline-boundary kinds, C every other kind
+#ifndef PL_PART
+#define PL_STEP_A 1
+#define PL_STEP_B 1
+#define PL_STEP_C 1
+#define PL_PART_AUX 1
+#define PL_PART_SIDE 1
+#else
+#define PL_STEP_A (PL_PART == 1)
+#define PL_STEP_B (PL_PART == 4)
+#define PL_STEP_C (PL_PART == 5)
+#define PL_PART_AUX (PL_PART == 2)
+#define PL_PART_SIDE (PL_PART == 3)
+#endif
+#define PL_PART_STEP (PL_STEP_A || PL_STEP_B || PL_STEP_C)
+
+#if PL_PART_SIDE
 
 // collide of a runtime kind (uniform over the grid), for the boundary kernels
 static __device__ __forceinline__ void collide_any(int kind, TC *f, TC *g, int idx, const KArgs &a, bool save, TC *u) {
@@ -146,9 +169,28 @@ static __global__ void __launch_bounds__(32 * kPostWarps) k_bnd_post_stream(KArg
     }
 }
 
+// the side-stream chains: the direct nodes on `side`, the staged nodes (pre -> post) on `side2`
+void PL_CAT(side_step_, PL_NAME)(const KArgs &a, int kind, cudaStream_t side, cudaStream_t side2) {
+    if (a.ndir > 0) k_bnd_direct<<<(a.ndir + 127) / 128, 128, 0, side>>>(a, kind);
+    if (a.ns > 0) {
+        k_bnd_pre<<<(a.ns + 127) / 128, 128, 0, side2>>>(a);
+        if (a.nt > 0) k_bnd_post<<<(a.nt + kPostWarps - 1) / kPostWarps, 32 * kPostWarps, 0, side2>>>(a, kind);
+    }
+}
+void PL_CAT(side_stream_, PL_NAME)(const KArgs &a, cudaStream_t side, cudaStream_t side2) {
+    if (a.ndir > 0) k_bnd_direct_stream<<<(a.ndir + 127) / 128, 128, 0, side>>>(a);
+    if (a.ns > 0) {
+        k_bnd_pre<<<(a.ns + 127) / 128, 128, 0, side2>>>(a);
+        if (a.nt > 0) k_bnd_post_stream<<<(a.nt + kPostWarps - 1) / kPostWarps, 32 * kPostWarps, 0, side2>>>(a);
+    }
+}
+#endif  // PL_PART_SIDE
+
 static dim3 interior_grid(const Geo &g) {
     return dim3((g.nx + 31) / 32, (g.ny + 7) / 8, PL_LAT::ND == 2 ? 1 : g.nz);
 }
+
+#if PL_PART_STEP
 
 // the pull part of a fused step
 template <int K>
@@ -169,11 +211,7 @@ static void run_kind(int op, bool save, const KArgs &a, cudaStream_t st) {
             cudaEventRecord(static_cast<cudaEvent_t>(a.ev_fork), st);
             cudaStreamWaitEvent(side, static_cast<cudaEvent_t>(a.ev_fork), 0);
             cudaStreamWaitEvent(side2, static_cast<cudaEvent_t>(a.ev_fork), 0);
-            if (a.ndir > 0) k_bnd_direct<<<(a.ndir + 127) / 128, 128, 0, side>>>(a, K);
-            if (a.ns > 0) {
-                k_bnd_pre<<<(a.ns + 127) / 128, 128, 0, side2>>>(a);
-                if (a.nt > 0) k_bnd_post<<<(a.nt + kPostWarps - 1) / kPostWarps, 32 * kPostWarps, 0, side2>>>(a, K);
-            }
+            PL_CAT(side_step_, PL_NAME)(a, K, side, side2);
             launch_pull<K>(a, st);
             cudaEventRecord(static_cast<cudaEvent_t>(a.ev_join), side);
             cudaEventRecord(static_cast<cudaEvent_t>(a.ev_join2), side2);
@@ -193,12 +231,29 @@ static void run_kind(int op, bool save, const KArgs &a, cudaStream_t st) {
     }
 }
 
-int PL_CAT(launch_, PL_NAME)(int kind, int op, bool save, const KArgs &a, cudaStream_t st) {
+#if PL_STEP_A
+static int launch_group_a(int kind, int op, bool save, const KArgs &a, cudaStream_t st) {
     switch (kind) {
     case K_AD_NATURAL: run_kind<K_AD_NATURAL>(op, save, a, st); return 0;
     case K_AD_FORCE: run_kind<K_AD_FORCE>(op, save, a, st); return 0;
+    default: return -1;
+    }
+}
+#endif
+
+#if PL_STEP_B
+int PL_CAT(launch_adj_, PL_NAME)(int kind, int op, bool save, const KArgs &a, cudaStream_t st) {
+    switch (kind) {
     case K_AAD_NATURAL: run_kind<K_AAD_NATURAL>(op, save, a, st); return 0;
     case K_AAD_FORCE: run_kind<K_AAD_FORCE>(op, save, a, st); return 0;
+    default: return -1;
+    }
+}
+#endif
+
+#if PL_STEP_C
+int PL_CAT(launch_misc_, PL_NAME)(int kind, int op, bool save, const KArgs &a, cudaStream_t st) {
+    switch (kind) {
     case K_NS_COLLIDE: run_kind<K_NS_COLLIDE>(op, save, a, st); return 0;
 #ifdef PL_ALL_KINDS
     case K_NS_BRINKMAN: run_kind<K_NS_BRINKMAN>(op, save, a, st); return 0;
@@ -222,7 +277,20 @@ int PL_CAT(launch_, PL_NAME)(int kind, int op, bool save, const KArgs &a, cudaSt
     default: return -1;
     }
 }
+#endif
 
+#if PL_STEP_A
+// every kind built for this (lattice, storage): the three groups in turn; -1 = not built
+int PL_CAT(launch_, PL_NAME)(int kind, int op, bool save, const KArgs &a, cudaStream_t st) {
+    if (launch_group_a(kind, op, save, a, st) == 0) return 0;
+    if (PL_CAT(launch_adj_, PL_NAME)(kind, op, save, a, st) == 0) return 0;
+    return PL_CAT(launch_misc_, PL_NAME)(kind, op, save, a, st);
+}
+#endif
+
+#endif  // PL_PART_STEP
+
+#if PL_PART_AUX
 void PL_CAT(aux_, PL_NAME)(int op, const KArgs &a, int which, const double *const *in, int has_g, int sgn,
                            double *host_or_dev, int set, double shift, cudaStream_t st) {
     const int n = a.geo.n;
@@ -234,11 +302,7 @@ void PL_CAT(aux_, PL_NAME)(int op, const KArgs &a, int which, const double *cons
             cudaEventRecord(static_cast<cudaEvent_t>(a.ev_fork), st);
             cudaStreamWaitEvent(side, static_cast<cudaEvent_t>(a.ev_fork), 0);
             cudaStreamWaitEvent(side2, static_cast<cudaEvent_t>(a.ev_fork), 0);
-            if (a.ndir > 0) k_bnd_direct_stream<<<(a.ndir + 127) / 128, 128, 0, side>>>(a);
-            if (a.ns > 0) {
-                k_bnd_pre<<<(a.ns + 127) / 128, 128, 0, side2>>>(a);
-                if (a.nt > 0) k_bnd_post_stream<<<(a.nt + kPostWarps - 1) / kPostWarps, 32 * kPostWarps, 0, side2>>>(a);
-            }
+            PL_CAT(side_stream_, PL_NAME)(a, side, side2);
             k_interior_stream<PL_LAT, PL_STORE><<<interior_grid(a.geo), dim3(32, 8), 0, st>>>(a, sgn);
             cudaEventRecord(static_cast<cudaEvent_t>(a.ev_join), side);
             cudaEventRecord(static_cast<cudaEvent_t>(a.ev_join2), side2);
@@ -266,5 +330,6 @@ void PL_CAT(aux_, PL_NAME)(int op, const KArgs &a, int which, const double *cons
     }
     }
 }
+#endif  // PL_PART_AUX
 
 }  // namespace pl

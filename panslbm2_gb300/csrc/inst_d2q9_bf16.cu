@@ -1,6 +1,6 @@
-// Kernel instantiations for D2Q9 with __nv_bfloat16 population storage.
+// Kernel instantiations for D2Q9 with __nv_bfloat16 population storage: the launch switch and the collide and fused-step launches of the forward inline-boundary kinds.
 #define PL_LAT D2Q9
 #define PL_STORE __nv_bfloat16
 #define PL_NAME d2q9_bf16
-
+#define PL_PART 1
 #include "inst_body.cuh"

@@ -1,0 +1,6 @@
+// Kernel instantiations for D2Q9 with __nv_bfloat16 population storage: the auxiliary launches (standalone stream, init, host transfer).
+#define PL_LAT D2Q9
+#define PL_STORE __nv_bfloat16
+#define PL_NAME d2q9_bf16
+#define PL_PART 2
+#include "inst_body.cuh"

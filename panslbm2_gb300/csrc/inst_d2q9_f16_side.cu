@@ -1,0 +1,6 @@
+// Kernel instantiations for D2Q9 with __half population storage: the side-stream boundary kernels.
+#define PL_LAT D2Q9
+#define PL_STORE __half
+#define PL_NAME d2q9_f16
+#define PL_PART 3
+#include "inst_body.cuh"

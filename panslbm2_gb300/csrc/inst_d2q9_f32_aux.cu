@@ -1,0 +1,9 @@
+// Kernel instantiations for D2Q9 with float population storage: the auxiliary launches (standalone stream, init, host transfer).
+#define PL_LAT D2Q9
+#define PL_STORE float
+#define PL_NAME d2q9_f32
+#define PL_ALL_KINDS
+#define PL_INCOMPRESSIBLE
+#define PL_ELASTIC
+#define PL_PART 2
+#include "inst_body.cuh"

@@ -1,0 +1,9 @@
+// Kernel instantiations for D2Q9 with double population storage: the collide and fused-step launches of the adjoint inline-boundary kinds.
+#define PL_LAT D2Q9
+#define PL_STORE double
+#define PL_NAME d2q9_f64
+#define PL_ALL_KINDS
+#define PL_INCOMPRESSIBLE
+#define PL_ELASTIC
+#define PL_PART 4
+#include "inst_body.cuh"

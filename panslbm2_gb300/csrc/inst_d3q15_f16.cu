@@ -1,6 +1,6 @@
-// Kernel instantiations for D3Q15 with __half population storage.
+// Kernel instantiations for D3Q15 with __half population storage: the launch switch and the collide and fused-step launches of the forward inline-boundary kinds.
 #define PL_LAT D3Q15
 #define PL_STORE __half
 #define PL_NAME d3q15_f16
-
+#define PL_PART 1
 #include "inst_body.cuh"

@@ -1,6 +1,7 @@
-// Kernel instantiations for D3Q15 with double population storage.
+// Kernel instantiations for D3Q15 with double population storage: the launch switch and the collide and fused-step launches of the forward inline-boundary kinds.
 #define PL_LAT D3Q15
 #define PL_STORE double
 #define PL_NAME d3q15_f64
 #define PL_ALL_KINDS
+#define PL_PART 1
 #include "inst_body.cuh"

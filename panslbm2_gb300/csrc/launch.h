@@ -9,8 +9,12 @@ enum AuxOp { AUX_STREAM_PROGRAM = 0, AUX_INIT = 1, AUX_DECODE = 2, AUX_ENCODE = 
 
 #define PL_DECL(name)                                                                                   \
     int launch_##name(int kind, int op, bool save, const KArgs &a, cudaStream_t st);                     \
+    int launch_adj_##name(int kind, int op, bool save, const KArgs &a, cudaStream_t st);                 \
+    int launch_misc_##name(int kind, int op, bool save, const KArgs &a, cudaStream_t st);                \
     void aux_##name(int op, const KArgs &a, int which, const double *const *in, int has_g, int sgn,     \
-                    double *buf, int set, double shift, cudaStream_t st);
+                    double *buf, int set, double shift, cudaStream_t st);                                \
+    void side_step_##name(const KArgs &a, int kind, cudaStream_t side, cudaStream_t side2);             \
+    void side_stream_##name(const KArgs &a, cudaStream_t side, cudaStream_t side2);
 PL_DECL(d2q9_f64)
 PL_DECL(d2q9_f32)
 PL_DECL(d2q9_f16)
