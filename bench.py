@@ -722,17 +722,22 @@ def main():
                        "l2": "inputs larger than L2: two population buffers of %.0f MB each" % pop_mb},
             "roofline": roof, "e2e": e2e, "clocks": ck, "gpu_launches": int(l1 - l0)}
     lp.close()
-    if rank == 0 and not args.no_design:
+    # the configuration legs and the CPU baseline run on one GPU only (N = 1): under torchrun
+    # the whole job's GPUs would otherwise wait for rank 0's minutes of single-GPU legs
+    legs = rank == 0 and world == 1
+    if world > 1 and rank == 0:
+        line["legs"] = "configuration legs and cpu_baseline: single-GPU runs only"
+    if legs and not args.no_design:
         leg(line, "config1_cavity", cavity_leg) if not args.no_cpu else None
         leg(line, "design_iter", design_leg, cpu=not args.no_cpu)
         leg(line, "design_iter_3d_surrogate", surrogate_leg)
         leg(line, "precision_errors", precision_leg)
         leg(line, "fp64_roofline", fp64_leg)
         leg(line, "dropin", dropin_leg)
-    if rank == 0 and not args.no_transient:
+    if legs and not args.no_transient:
         leg(line, "transient_iter", transient_gpu)
         leg(line, "transient_precision", transient_precision)
-    if rank == 0 and not args.no_cpu:
+    if legs and not args.no_cpu:
         line["cpu_baseline"] = cpu_port(S)
     if rank == 0:
         print(json.dumps(line), flush=True)
