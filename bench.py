@@ -18,7 +18,7 @@ step over the whole lattice: pull-stream + boundary program + collide. The popul
                  read alpha, kappa and the heat source) / measured step time, vs MEASURED_PEAKS
   cpu_baseline   the C restatement of the reference's scalar OpenMP path (oracle/), FP64, on the
                  host cores: one warm-up step, then the median of 5 timed spans
-  config1_cavity the 100x100 lid-driven cavity, 20,000 steps, FP64, GPU and the CPU port timed,
+  cavity_100x100 the 100x100 lid-driven cavity, 20,000 steps, FP64, GPU and the CPU port timed,
                  and their largest difference
   design_iter    one design iteration of the 200x100 FP64 forced-convection heat sink (filter,
                  forward and adjoint to residual 1e-6, sensitivity, filtered sensitivity) on the
@@ -236,7 +236,7 @@ def cpu_port(S, spans=5, steps_per_span=None, budget_s=12.0):
 
 
 def cavity_leg():
-    """config 1: the 100x100 lid-driven cavity, 20,000 steps, FP64: GPU and CPU port"""
+    """the 100x100 lid-driven cavity, 20,000 steps, FP64: GPU and CPU port"""
     from oracle.olib import Oracle
     from panslbm2_gb300 import forced as FC
     from tests import _forced_oracle as FO
@@ -256,7 +256,7 @@ def cavity_leg():
 
 
 def design_leg(cpu=True, cpu_budget_s=120.0):
-    """config 2: one forced-convection design iteration on 200x100 FP64 (filter, forward and
+    """one forced-convection design iteration on 200x100 FP64 (filter, forward and
     adjoint to 1e-6, sensitivity, filtered sensitivity); the CPU port's forward + adjoint on the
     same step counts"""
     from panslbm2_gb300 import _capi as A
@@ -343,7 +343,7 @@ def design_cpu(p, ss, nf, na, budget_s):
 
 
 def surrogate_leg(tol=1e-5, seeds=(0, 1, 2, 3, 4), max_steps=40000, fallback=20000):
-    """config 4: plain vs learned warm start on 160x160x80 FP32, held-out designs (seeds 0-4; the
+    """plain vs learned warm start on the 160x160x80 FP32 forced heat sink, held-out designs (seeds 0-4; the
     training designs are seeds 1000 and up). Warm starts: "both" seeds the forward and the
     adjoint problems (a seeded adjoint not converged after `fallback` steps restarts from rest),
     "forward" seeds the forward problem only."""
@@ -394,7 +394,7 @@ def surrogate_leg(tol=1e-5, seeds=(0, 1, 2, 3, 4), max_steps=40000, fallback=200
 
 
 def precision_leg(nf=4000, na=4000):
-    """config 3: FP32 / FP16 / BF16 storage against FP64 on the 1600x800 forced heat sink"""
+    """FP32 / FP16 / BF16 storage against FP64 on the 1600x800 forced heat sink"""
     from panslbm2_gb300 import forced as FC
     p = FC.ForcedParams(2, 1600, 800)
     s = p.design(seed=0)
@@ -549,7 +549,7 @@ TRANSIENT_LATTICE = dict(nd=3, lx=192, ly=192, lz=96, storage="fp32", levels=400
 
 
 def transient_gpu():
-    """One transient evaluation of the forced-convection heat sink (config 5 physics: base-plate
+    """One transient evaluation of the forced-convection heat sink (base-plate
     source, inflow u(t) = 0.02 (1 - exp(-t / 500))): forward from rest over 4000 time levels, the
     adjoint swept back with its sensitivity terms per step, checkpoints every 100 steps recomputed
     on the device, on the 192x192x96 FP32 lattice, through panslbm2_gb300.transient."""
@@ -575,9 +575,9 @@ def transient_gpu():
 
 
 def transient_precision(levels=400, every=50):
-    """The fifth configuration's lattice (192x192x96, forced physics, u(t)) over the first
+    """The transient heat-sink lattice (192x192x96, forced physics, u(t)) over the first
     `levels` time levels, FP32 against FP64: objective and sensitivity errors of the transient
-    sweep at configuration size (the full 4000 levels in FP64 would take minutes)."""
+    sweep at full lattice size (the full 4000 levels in FP64 would take minutes)."""
     from panslbm2_gb300 import forced as FC
     from panslbm2_gb300.transient import TransientHeatSink
     d = TRANSIENT_LATTICE
@@ -728,7 +728,7 @@ def main():
     if world > 1 and rank == 0:
         line["legs"] = "configuration legs and cpu_baseline: single-GPU runs only"
     if legs and not args.no_design:
-        leg(line, "config1_cavity", cavity_leg) if not args.no_cpu else None
+        leg(line, "cavity_100x100", cavity_leg) if not args.no_cpu else None
         leg(line, "design_iter", design_leg, cpu=not args.no_cpu)
         leg(line, "design_iter_3d_surrogate", surrogate_leg)
         leg(line, "precision_errors", precision_leg)

@@ -1,5 +1,5 @@
-"""The topology-optimisation loop of the forced-convection heat sink (the second configuration:
-200 x 100, FP64, 20 design iterations), on one device lattice and the device MMA.
+"""The topology-optimisation loop of the forced-convection heat sink (200 x 100, FP64, 20 design
+iterations), on one device lattice and the device MMA.
 
 Each design iteration takes the steps of production/heatsink.cpp:93-280, with this problem's
 physics (panslbm2_gb300.forced):
@@ -15,8 +15,8 @@ physics (panslbm2_gb300.forced):
      0.2 (:74-81, :263), base plate cells held at 0;
   7. the largest design change dsmax (:264-283).
 
-The reference's continuation over (qf, beta) stages is not part of the configuration; beta and
-the filter radius stay at the configuration's values.
+The reference's continuation over (qf, beta) stages is not part of this loop; beta and the
+filter radius stay at the problem's values (ForcedParams).
 """
 import json
 import time
@@ -83,7 +83,7 @@ class ForcedOptimisation:
 
 def main(argv=None):
     """python -m panslbm2_gb300.optimize [--shape X,Y] [--iterations K] [--storage fp64]:
-    the second configuration's optimisation loop from the seeded GRF design 0"""
+    the forced heat sink's optimisation loop from the seeded GRF design 0"""
     import argparse
     ap = argparse.ArgumentParser()
     ap.add_argument("--shape", default="200,100")
