@@ -11,6 +11,7 @@
 #include <cmath>
 #include <map>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include <nvtx3/nvToolsExt.h>
@@ -440,6 +441,9 @@ int compile_program(pl_lattice h, const pl_bc_desc *descs, int ndesc, Program &P
         // apply go to the side path; other op nodes are applied inline (inline kinds) or by
         // the direct kernel (other kinds)
         icode.assign(h->n, -1);
+        // nodes with the same ops and values share one record (walls, fluxes): fewer distinct
+        // records for the face lanes of a warp to read
+        std::unordered_map<std::string, int> rec_index;
         for (size_t sl = 0; sl < opnodes.size(); ++sl) {
             const int node = opnodes[sl];
             if (is_t[node]) { icode[node] = -2; continue; }
@@ -462,8 +466,13 @@ int compile_program(pl_lattice h, const pl_bc_desc *descs, int ndesc, Program &P
                     rec.val[m][3] = op.eps;
                 }
                 rec.nops = (uint32_t)(bstart[sl + 1] - bstart[sl]);
-                icode[node] = (int)irec.size();
-                irec.push_back(rec);
+                const std::string key(reinterpret_cast<const char *>(&rec), sizeof rec);
+                auto it = rec_index.find(key);
+                if (it == rec_index.end()) {
+                    it = rec_index.emplace(key, (int)irec.size()).first;
+                    irec.push_back(rec);
+                }
+                icode[node] = it->second;
             } else {
                 icode[node] = -2;
             }
